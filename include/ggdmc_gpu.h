@@ -1,0 +1,268 @@
+/*
+ * ggdmc_gpu.h -- C ABI of the GB300 DE-MCMC sampler (ggdmc's sampling hot path).
+ *
+ * The reference crosses from R into C++ through three .Call entry points
+ * registered in src/RcppExports.cpp:54-59:
+ *
+ *   _ggdmc_run_subject(config, dmi,  samples)  -> src/de2R.cpp:8-23
+ *   _ggdmc_run_hyper  (config, dmi,  samples)  -> src/de2R.cpp:30-47
+ *   _ggdmc_run        (config, dmis, samples)  -> src/de2R.cpp:123-171
+ *
+ * Each unpacks S4 slots into ggdmcHeaders objects, runs de_class
+ * (run_chains / run_hchains, src/de.cpp) and wraps theta_class storage into S4
+ * `posterior` objects (src/type_casting.h:10-25).  This header is the same
+ * boundary with plain C types: a .Call shim (or ctypes / cffi) converts the S4
+ * slots into the POD structs below, calls one function, and copies the sample
+ * arrays back into `posterior` slots.  The array layouts equal R's
+ * column-major ones, so that copy is a memcpy.
+ *
+ * All pointers are HOST pointers owned by the caller.  Functions return a
+ * ggdmc_status (0 = success) and never abort; ggdmc_last_error() gives the
+ * message of the calling thread's last failure.
+ */
+#ifndef GGDMC_GPU_H
+#define GGDMC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum {
+    GGDMC_OK = 0,
+    GGDMC_ERR_ARG = 1,      /* invalid argument or unsupported model       */
+    GGDMC_ERR_CUDA = 2,     /* a CUDA runtime call failed                   */
+    GGDMC_ERR_TIMEOUT = 3,  /* the device did not finish within the limit   */
+    GGDMC_ERR_NUMERIC = 4,  /* a device-side check flagged bad numerics     */
+    GGDMC_ERR_NOMEM = 5     /* device or host allocation failed             */
+} ggdmc_status;
+
+/* ------------------------------------------------------- enumerations */
+enum { GGDMC_MODEL_LBA = 0, GGDMC_MODEL_DDM = 1 };
+
+/* Arithmetic of the likelihood kernels.
+ *  FP64        -- every step in double; the parity path.
+ *  MIXED       -- per-trial densities in FP32 with FP64 re-evaluation of the
+ *                 trials whose FP32 form is ill-conditioned; per-chain sums,
+ *                 priors and the Metropolis difference in FP64.
+ *  FP64_PLAIN  -- double throughout, one launch per subject per pass: the
+ *                 plain GPU form the batched kernels are measured against. */
+enum { GGDMC_FP64 = 0, GGDMC_MIXED = 1, GGDMC_FP64_PLAIN = 2 };
+
+/* Prior families, ggdmcPrior's dist_id codes (fixture lba_data*.rda). */
+enum { GGDMC_PRIOR_TNORM = 1, GGDMC_PRIOR_UNIF = 6 };
+
+/* Number of parameter kinds per accumulator (LBA: A, B, mean_v, sd_v, t0,
+ * st0) and per response (DDM: a, v, z, d, sz, sv, t0, st0). */
+#define GGDMC_LBA_NKIND 6
+#define GGDMC_DDM_NKIND 8
+
+/* ------------------------------------------------------------- structs */
+
+/* A design, flattened from ggdmcModel's `model` + a DMI's node_1_index.
+ * param_src[(c*n_acc + k)*n_kind + q] >= 0 indexes theta; < 0 is -1-j into
+ * constants.  resp[c] is the responding accumulator (node 1) of cell c. */
+typedef struct {
+    int32_t model_type;        /* GGDMC_MODEL_LBA / GGDMC_MODEL_DDM */
+    int32_t n_par;             /* free parameters per subject       */
+    int32_t n_cell;
+    int32_t n_acc;             /* LBA accumulators; DDM: 2 boundaries */
+    int32_t n_kind;            /* GGDMC_LBA_NKIND / GGDMC_DDM_NKIND   */
+    int32_t n_const;
+    const int32_t *param_src;  /* [n_cell][n_acc][n_kind] */
+    const int32_t *resp;       /* [n_cell]                */
+    const double *constants;   /* [n_const]               */
+} ggdmc_model;
+
+/* Trials of n_subject subjects packed back to back (dmi@data, cell-grouped). */
+typedef struct {
+    int32_t n_subject;
+    const int64_t *offsets;    /* [n_subject + 1]          */
+    const double *rt;          /* [offsets[n_subject]] (s) */
+    const int32_t *cell;       /* [offsets[n_subject]]     */
+} ggdmc_data;
+
+/* One ggdmcPrior p_prior / h_prior list: per parameter
+ * (p0, p1, lower, upper, dist_id, log_p). */
+typedef struct {
+    int32_t n_par;
+    const double *table;       /* [n_par][6] */
+} ggdmc_prior;
+
+/* de_input + theta_input (R/model-class.R:1288-1313, 36-57). */
+typedef struct {
+    double pop_migration_prob;
+    double sub_migration_prob;
+    double gamma_precursor;    /* 2.38 */
+    double rp;                 /* 0.001 */
+    int32_t is_hblocked;
+    int32_t is_pblocked;
+    int32_t nparameter;        /* de_input@nparameter: gamma = g0/sqrt(2*nparameter) */
+    int32_t nchain;
+    int32_t nmc;               /* stored samples, slot 0 = start state */
+    int32_t thin;              /* iterations between stored samples    */
+    int32_t precision;         /* GGDMC_FP64 / GGDMC_MIXED / GGDMC_FP64_PLAIN */
+    int32_t flags;             /* reserved, 0 */
+    uint64_t seed;             /* key of the counter-based draw stream */
+} ggdmc_de_config;
+
+/* Current chain state of one level (theta_class m_used_theta/lp/ll). */
+typedef struct {
+    double *theta;             /* [nchain][npar] == R [npar, nchain] */
+    double *lp;                /* [nchain] */
+    double *ll;                /* [nchain] */
+} ggdmc_chain_state;
+
+/* Thinned samples of one level: posterior@theta, @summed_log_prior,
+ * @log_likelihoods (R/phi.R:77-87). */
+typedef struct {
+    double *theta;             /* [nmc][nchain][npar] == R [npar, nchain, nmc] */
+    double *lp;                /* [nmc][nchain]       == R [nchain, nmc]       */
+    double *ll;                /* [nmc][nchain]                                */
+} ggdmc_samples;
+
+/* Acceptance counters of one run (reported, not needed for results). */
+typedef struct {
+    int64_t proposals;
+    int64_t accepts;
+    int64_t migrations;        /* migration passes taken      */
+    int64_t reevaluations;     /* speculative re-evaluations  */
+    int64_t kernel_launches;   /* kernels launched by the run */
+} ggdmc_run_stats;
+
+typedef struct ggdmc_handle ggdmc_handle;
+
+/* ------------------------------------------------------ canonical draws
+ * Every uniform the sampler consumes is keyed by (iteration, level, pass,
+ * slot).  level 0 is the single level of run_subject / run_hyper or the phi
+ * level of run; level 1+s is subject s of run.  pass is 0, or the blocked
+ * parameter index.  With draws == NULL the uniforms come from Philox4x32-10
+ * keyed by cfg->seed; otherwise draws[] holds them at
+ *   ((((iter-1)*n_level + level)*n_pass + pass)*n_slot + slot)
+ * for iter = 1 .. n_iter.  ggdmc_draw_layout() returns the four extents.
+ *
+ * Within one (iter, level, pass), with C = nchain and Pn = cfg->nparameter:
+ *   slot 0                    migration-vs-crossover selector
+ *   slot 1                    migration subset proportion
+ *   slot 2 .. C+1             migration subset picks (partial Fisher-Yates)
+ *   base(i) = 2 + C + i*(Pn+3), chain i of a crossover / step i of a
+ *   migration: base+0, base+1 partner picks; base+2+j jitter of parameter j;
+ *   base+2+Pn the Metropolis accept uniform. */
+#define GGDMC_DRAW_SLOTS(nchain, nparameter) \
+    (2 + (int64_t)(nchain) + (int64_t)(nchain) * ((int64_t)(nparameter) + 3))
+ggdmc_status ggdmc_draw_layout(const ggdmc_de_config *cfg, int32_t n_level,
+                               int32_t hierarchical,
+                               int64_t *n_iter, int64_t *n_pass,
+                               int64_t *n_slot, int64_t *total);
+
+/* ---------------------------------------------------- entry points */
+
+/* run_subject (src/de2R.cpp:8-23, .Call _ggdmc_run_subject): DE-MCMC of one
+ * subject; `state` is the start (slot 0) and receives the final state. */
+ggdmc_status ggdmc_run_subject(const ggdmc_de_config *cfg,
+                               const ggdmc_model *model,
+                               const ggdmc_data *data,       /* n_subject == 1 */
+                               const ggdmc_prior *p_prior,
+                               ggdmc_chain_state *state,
+                               const double *draws,          /* NULL: Philox */
+                               ggdmc_samples *out,
+                               ggdmc_run_stats *stats);      /* nullable */
+
+/* run_hyper (src/de2R.cpp:30-47, .Call _ggdmc_run_hyper): phi-only DE-MCMC
+ * whose likelihood is the truncated-normal density of a fixed subject-by-
+ * parameter matrix (hyper_dmi@data, row-major [n_row][p_prior->n_par]). */
+ggdmc_status ggdmc_run_hyper(const ggdmc_de_config *cfg,
+                             const double *hyper_data, int32_t n_row,
+                             const ggdmc_prior *p_prior,
+                             const ggdmc_prior *h_prior,
+                             ggdmc_chain_state *state,
+                             const double *draws,
+                             ggdmc_samples *out,
+                             ggdmc_run_stats *stats);
+
+/* run (src/de2R.cpp:123-171, .Call _ggdmc_run): hierarchical DE-MCMC,
+ * phi level + data->n_subject subjects.  subj_state[s] / subj_out[s] per
+ * subject. */
+ggdmc_status ggdmc_run(const ggdmc_de_config *cfg,
+                       const ggdmc_model *model,
+                       const ggdmc_data *data,
+                       const ggdmc_prior *p_prior,
+                       const ggdmc_prior *h_prior,
+                       ggdmc_chain_state *phi_state,
+                       ggdmc_chain_state *subj_state,
+                       const double *draws,
+                       ggdmc_samples *phi_out,
+                       ggdmc_samples *subj_out,
+                       ggdmc_run_stats *stats);
+
+/* Many independent run_subject fits in one launch sequence (the reference
+ * runs them as separate R processes, R/sampling.R:13-121).  Fit f uses the
+ * data of subject f, p_prior, state[f], out[f]; level f keys its draws. */
+ggdmc_status ggdmc_run_subjects(const ggdmc_de_config *cfg,
+                                const ggdmc_model *model,
+                                const ggdmc_data *data,
+                                const ggdmc_prior *p_prior,
+                                ggdmc_chain_state *state,
+                                const double *draws,
+                                ggdmc_samples *out,
+                                ggdmc_run_stats *stats);
+
+/* ------------------------------------------------- resident handle API
+ * Upload a design and its trials once; run repeatedly (RestartSampling).  */
+ggdmc_status ggdmc_create(const ggdmc_model *model, const ggdmc_data *data,
+                          ggdmc_handle **out);
+ggdmc_status ggdmc_destroy(ggdmc_handle *h);
+
+/* Per-subject log-likelihood sums of n_theta parameter vectors per subject:
+ * theta [n_subject][n_theta][n_par] -> out [n_subject][n_theta].
+ * This is LPtr->sumloglike (called at src/de.cpp:145,187,604,653) batched. */
+ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta,
+                          int32_t precision, double *out);
+
+/* The same with theta and out already in device memory (CUDA pointers) and
+ * the launch on `stream` (a cudaStream_t; NULL = the default stream). */
+ggdmc_status ggdmc_loglik_device(ggdmc_handle *h, const double *d_theta,
+                                 int32_t n_theta, int32_t precision,
+                                 double *d_out, void *stream);
+
+/* Per-trial log densities of one parameter vector per subject (the terms
+ * sumloglike adds): theta [n_subject][n_par] -> out [total trials]. */
+ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta,
+                                 int32_t precision, double *out);
+
+/* sumlogprior (ggdmcPrior, called at src/de.cpp:144,186,603,652):
+ * theta [n][n_par] -> out [n]. */
+ggdmc_status ggdmc_logprior(const ggdmc_prior *prior, const double *theta,
+                            int32_t n, double *out);
+
+/* sumloghlike (src/de.cpp:245-270): phi [n][2P], subject thetas
+ * [n_subject][n][P] (chain j of every subject pairs with phi j) -> out [n]. */
+ggdmc_status ggdmc_loghlike(const ggdmc_prior *p_prior, const double *phi,
+                            const double *subj_theta, int32_t n_subject,
+                            int32_t n, double *out);
+
+/* Run on a resident handle: level layout as ggdmc_run (phi_state == NULL
+ * runs the subjects as independent fits, like ggdmc_run_subjects). */
+ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg,
+                              const ggdmc_prior *p_prior,
+                              const ggdmc_prior *h_prior,
+                              ggdmc_chain_state *phi_state,
+                              ggdmc_chain_state *subj_state,
+                              const double *draws,
+                              ggdmc_samples *phi_out,
+                              ggdmc_samples *subj_out,
+                              ggdmc_run_stats *stats);
+
+/* Message of this thread's last failed call ("" if none). */
+const char *ggdmc_last_error(void);
+
+/* Library version string. */
+const char *ggdmc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GGDMC_GPU_H */
