@@ -1,0 +1,348 @@
+"""Benchmark of the DE-MCMC hot path on one GB300.
+
+Workload: the uneven 256-subject hierarchical LBA (N_s ~ U{100..2000}, the
+17-parameter 4-accumulator design, 51 chains, theta ~ tnorm(pop, 10% CV)).
+A step is one DE sweep: the phi level and every subject, all chains
+(src/de.cpp:272-383).  Metric: DE sweeps/s (with trial-logL evals/s beside
+it), batched mixed precision, exact reference chain order.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's algorithm on the host cores: the
+CPU restatement in oracle/ (the reference itself needs R and packages that
+are not installable here), one replica per host thread, as the reference's
+own parallelism runs independent instances (R/sampling.R:13-121).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from ggdmc_gb300 import abi, synth  # noqa: E402
+
+WORKLOAD = "uneven_lba_256"
+K_ACC = 4
+FLOPS_PER_EVAL = 17 * K_ACC + 2          # algorithmic flops of one LBA trial density
+TRANS_PER_EVAL = 4 * K_ACC + 1           # Phi / phi / log evaluations
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return False
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+        return False
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_workload():
+    t = time.time()
+    w = synth.uneven_lba_256()
+    log(f"workload {w.name}: {w.batch.n_subject} subjects, {len(w.batch.rt)} trials, "
+        f"{w.nchain} chains ({time.time() - t:.1f}s to simulate)")
+    return w
+
+
+def start_state(w, gpu, h):
+    rng = np.random.default_rng(12)
+    C_ = w.nchain
+    th, phi = synth.start_states(w, C_, rng)
+    S = w.batch.n_subject
+    lp = np.stack([gpu.logprior(w.p_prior, th[s]) for s in range(S)])
+    ll = h.loglik(th, abi.FP64)
+    plp = gpu.logprior(w.h_prior, phi)
+    pll = gpu.loghlike(w.p_prior, phi, th.transpose(0, 1, 2))
+    return (phi, plp, pll), (th, lp, ll)
+
+
+def cfg_for(w, steps, precision, flags=0, seed=2025):
+    return abi.DEConfigPy(nchain=w.nchain, nparameter=2 * w.model.n_par, nmc=steps + 1, thin=1,
+                          pop_migration_prob=0.05, sub_migration_prob=0.06, precision=precision,
+                          seed=seed, flags=flags)
+
+
+def loglik_roofline(w, h, n_launch=10):
+    """Time the likelihood kernel live (CUDA events on its stream): all
+    subjects x 51 proposals per launch, the k_sub_loglik work of one sweep."""
+    import torch
+    rng = np.random.default_rng(5)
+    th, _ = synth.start_states(w, w.nchain, rng)
+    d_th = torch.from_numpy(np.ascontiguousarray(th)).cuda()
+    d_out = torch.empty((w.batch.n_subject, w.nchain), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        h.loglik_device(d_th.data_ptr(), w.nchain, d_out.data_ptr(), abi.MIXED, stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times = []
+    for i in range(n_launch):
+        flush.fill_(i & 0xff)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.loglik_device(d_th.data_ptr(), w.nchain, d_out.data_ptr(), abi.MIXED, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    evals = int(w.nchain * len(w.batch.rt))
+    return ms, evals
+
+
+def cpu_baseline(w, n_sweeps=1, threads=None):
+    """The oracle on the host cores: `threads` replicas, each n_sweeps sweeps
+    of the full workload (FP64, reference chain order)."""
+    from oracle import binding as ob
+    ob.build()
+    rng = np.random.default_rng(12)
+    th, phi = synth.start_states(w, w.nchain, rng)
+    S = w.batch.n_subject
+    lp = np.stack([ob.logprior(w.p_prior, th[s]) for s in range(S)])
+    ll = ob.loglik(w.model, w.batch, th)
+    plp = ob.logprior(w.h_prior, phi)
+    pll = ob.loghlike(w.p_prior, phi, th)
+    cfg = cfg_for(w, n_sweeps, abi.FP64)
+    threads = threads or os.cpu_count() or 1
+    times = [0.0] * threads
+
+    def one(k):
+        c = abi.DEConfigPy(**{**cfg.__dict__, "seed": 1000 + k})
+        t0 = time.perf_counter()
+        ob.run(c, w.model, w.batch, w.p_prior, w.h_prior, (phi, plp, pll), (th, lp, ll))
+        times[k] = time.perf_counter() - t0
+
+    ts = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
+    t0 = time.perf_counter()
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    wall = time.perf_counter() - t0
+    sweeps = threads * n_sweeps
+    return {"value": sweeps / wall, "unit": "DE sweeps/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} replicas x {n_sweeps} sweep(s) of the full {WORKLOAD} "
+                      f"workload, oracle/ FP64 C restatement, one thread each",
+            "wall_s": wall, "single_replica_s": float(np.median(times)),
+            "trial_logl_evals_per_s": sweeps * w.nchain * len(w.batch.rt) / wall}
+
+
+def run_ours(args):
+    import torch
+    from ggdmc_gb300 import build, gpu
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    build.build()
+    w = make_workload()
+    h = gpu.Handle(w.model, w.batch)
+    phi, subj = start_state(w, gpu, h)
+    peak_fp32, peak_mufu = gpu.probe_peaks()
+
+    # warm-up (also compiles nothing: the library is prebuilt)
+    wu = cfg_for(w, args.warmup, abi.MIXED, abi.FLAG_L2_FLUSH)
+    h.run(wu, w.p_prior, *subj, h_table=w.h_prior, phi=phi)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    cfg = cfg_for(w, args.steps, abi.MIXED, abi.FLAG_L2_FLUSH)
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        out = h.run(cfg, w.p_prior, *subj, h_table=w.h_prior, phi=phi)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    st = out["stats"]
+    ms = st["sweep_ms"]
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    sweeps_s = args.steps / (ms / 1e3)
+    evals_s = st["trial_evals"] / (st["sweep_ms"] / 1e3)
+
+    # plain FP64 one-launch-per-subject form (the comparison the target names)
+    n_plain = max(2, min(args.steps, 4))
+    pl = h.run(cfg_for(w, n_plain, abi.FP64_PLAIN, abi.FLAG_L2_FLUSH), w.p_prior, *subj,
+               h_table=w.h_prior, phi=phi)["stats"]
+    plain_sweeps_s = n_plain / (pl["sweep_ms"] / 1e3)
+    fb = h.run(cfg_for(w, n_plain, abi.FP64, abi.FLAG_L2_FLUSH), w.p_prior, *subj,
+               h_table=w.h_prior, phi=phi)["stats"]
+    fp64_sweeps_s = n_plain / (fb["sweep_ms"] / 1e3)
+
+    # likelihood kernel roofline (live)
+    lk_ms, lk_evals = loglik_roofline(w, h)
+    ach_tflops = lk_evals * FLOPS_PER_EVAL / (lk_ms * 1e-3) / 1e12
+    ach_mufu = lk_evals * TRANS_PER_EVAL / (lk_ms * 1e-3) / 1e12
+
+    # end to end through the one-shot C ABI with host buffers
+    t0 = time.perf_counter()
+    e2e = gpu.run(cfg_for(w, args.steps, abi.MIXED), w.model, w.batch, w.p_prior, w.h_prior,
+                  phi, subj)
+    e2e_s = time.perf_counter() - t0
+    S, Cn, P = w.batch.n_subject, w.nchain, w.model.n_par
+    h2d = (w.batch.rt.nbytes + w.batch.cell.nbytes + w.batch.offsets.nbytes
+           + subj[0].nbytes + subj[1].nbytes + subj[2].nbytes
+           + phi[0].nbytes + phi[1].nbytes + phi[2].nbytes)
+    d2h = 8 * (S * (args.steps + 1) * Cn * (P + 2) + (args.steps + 1) * Cn * (2 * P + 2)
+               + S * Cn * (P + 2) + Cn * (2 * P + 2))
+
+    line = {
+        "metric": "DE sweeps/s (trial-logL evals/s beside it), batched mixed FP32/FP64",
+        "value": round(sweeps_s * world, 3),
+        "unit": "DE sweeps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded LBA race simulation of the named shapes)",
+        "config": {"workload": WORKLOAD, "subjects": S, "trials": int(len(w.batch.rt)),
+                   "trials_per_subject": "U{100..2000}", "accumulators": K_ACC,
+                   "npar": P, "nphi": 2 * P, "chains": Cn, "pop_migration_prob": 0.05,
+                   "sub_migration_prob": 0.06, "chain_order": "reference (in place, in order)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "flushed between sweeps (256 MB memset, excluded from the timing)"},
+        "trial_logl_evals_per_s": round(evals_s * world, 1),
+        "fp64_plain_sweeps_per_s": round(plain_sweeps_s, 3),
+        "fp64_batched_sweeps_per_s": round(fp64_sweeps_s, 3),
+        "speedup_vs_fp64_plain": round(sweeps_s / plain_sweeps_s, 2),
+        "reevaluations_per_sweep": round(st["reevaluations"] / args.steps, 2),
+        "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
+        "gpu_launches": int(st["kernel_launches"]),
+        "roofline": {"kernel": "loglik (k_loglik_batch = k_sub_loglik body)",
+                     "bound": "fp32", "achieved": round(ach_tflops, 3),
+                     "peak": round(peak_fp32, 3), "unit": "TFLOP/s",
+                     "frac": round(ach_tflops / peak_fp32, 4), "traffic": None,
+                     "flops_per_eval": FLOPS_PER_EVAL, "evals_per_launch": lk_evals,
+                     "launch_ms": round(lk_ms, 4),
+                     "peak_source": "measured (ggdmc_probe_peaks FMA loop)",
+                     "sfu": {"achieved_tops": round(ach_mufu, 4), "peak_tops": round(peak_mufu, 4),
+                             "frac": round(ach_mufu / peak_mufu, 4),
+                             "transcendentals_per_eval": TRANS_PER_EVAL}},
+        "e2e": {"value": round(args.steps / e2e_s, 3), "unit": "DE sweeps/s",
+                "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps),
+                "call": "ggdmc_run (one-shot C ABI: upload, sweeps, sample download)"},
+        "clocks": clk.summary(),
+        "wall_s_timed_run": round(wall, 3),
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(w, 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = make_workload()
+    from oracle import binding as ob
+    ob.build()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    # each step: one sweep per replica, all host threads
+    vals = []
+    t_all = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 2))):
+        vals.append(cpu_baseline(w, 1, threads))
+    wall = time.perf_counter() - t_all
+    v = float(np.median([x["value"] for x in vals]))
+    line = {
+        "metric": "DE sweeps/s (trial-logL evals/s beside it), batched mixed FP32/FP64",
+        "value": round(v, 4), "unit": "DE sweeps/s", "impl": "reference",
+        "n_gpus": world, "steps": len(vals), "warmup": 0,
+        "ms_per_step": round(1e3 / v, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "subjects": w.batch.n_subject,
+                   "trials": int(len(w.batch.rt)), "chains": w.nchain},
+        "trial_logl_evals_per_s": round(float(np.median([x["trial_logl_evals_per_s"] for x in vals])), 1),
+        "cpu_baseline": {**vals[0], "value": round(v, 4)},
+        "e2e": {"value": round(v, 4), "unit": "DE sweeps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": round(wall, 2),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -20,6 +20,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_TIMEOUT",
 MODEL_LBA, MODEL_DDM = 0, 1
 FP64, MIXED, FP64_PLAIN = 0, 1, 2
 PRIOR_TNORM, PRIOR_UNIF = 1, 6
+FLAG_L2_FLUSH = 1
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -59,7 +60,9 @@ class Samples(C.Structure):
 
 class RunStats(C.Structure):
     _fields_ = [("proposals", C.c_int64), ("accepts", C.c_int64), ("migrations", C.c_int64),
-                ("reevaluations", C.c_int64), ("kernel_launches", C.c_int64)]
+                ("reevaluations", C.c_int64), ("kernel_launches", C.c_int64),
+                ("trial_evals", C.c_int64), ("iterations", C.c_int64), ("sweep_ms", C.c_double),
+                ("resolve_rounds", C.c_int64), ("resolve_finish", C.c_int64)]
 
 
 def dptr(a: np.ndarray):
@@ -146,12 +149,13 @@ class DEConfigPy:
     is_pblocked: bool = False
     precision: int = FP64
     seed: int = 0
+    flags: int = 0
 
     def to_c(self) -> DEConfig:
         return DEConfig(self.pop_migration_prob, self.sub_migration_prob, self.gamma_precursor,
                         self.rp, int(self.is_hblocked), int(self.is_pblocked),
                         self.nparameter, self.nchain, self.nmc, self.thin,
-                        self.precision, 0, self.seed & 0xFFFFFFFFFFFFFFFF)
+                        self.precision, self.flags, self.seed & 0xFFFFFFFFFFFFFFFF)
 
 
 def draw_slots(nchain: int, nparameter: int) -> int:

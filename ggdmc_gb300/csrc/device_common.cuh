@@ -1,0 +1,134 @@
+// device_common.cuh -- draws, normal functions and the per-trial LBA densities
+// shared by the sampler kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "model_tables.h"
+
+namespace ggdmc {
+
+// ----------------------------------------------------------------- draws
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11), counter = (slot, pass,
+// level, iteration), key = seed.  The 52-bit uniform ((m + 0.5) * 2^-52) is
+// exactly representable, so every consumer of a draw sees the same double.
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+        const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+}
+
+struct DrawSrc {
+    const double *draws;   // host-fed canonical array, or nullptr
+    uint64_t seed;
+    int64_t n_level, n_pass, n_slot;
+};
+
+__device__ __forceinline__ double uniform(const DrawSrc &d, int64_t it, int64_t level,
+                                          int64_t pass, int64_t slot)
+{
+    if (d.draws)
+        return d.draws[(((it - 1) * d.n_level + level) * d.n_pass + pass) * d.n_slot + slot];
+    uint32_t c[4] = {(uint32_t)slot, (uint32_t)pass, (uint32_t)level, (uint32_t)it};
+    philox4x32_10(c, (uint32_t)d.seed, (uint32_t)(d.seed >> 32));
+    const uint64_t m = ((uint64_t)c[0] << 20) | (c[1] >> 12);
+    return __dmul_rn((double)m + 0.5, 0x1p-52);
+}
+
+// -------------------------------------------------------------- normals
+__device__ __forceinline__ double Phi64(double z) { return 0.5 * erfc(-z * 0.70710678118654752440); }
+__device__ __forceinline__ double phi64(double z) { return exp(-0.5 * z * z) * 0.39894228040143267794; }
+__device__ __forceinline__ float phi32(float z) { return expf(-0.5f * z * z) * 0.398942280f; }
+
+// ------------------------------------------------------ FP64 LBA trial
+// The reference form (ggdmcLikelihood, restated): node-1 pdf floored at
+// 1e-10, t <= 0 gives 1e-10, a non-positive product gives DBL_EPSILON.
+// e64[u] = (A, b, v, s, Phi(v/s)) of unique accumulator tuple u.
+__device__ __forceinline__ double lba_logdens64(double t, const int *ents, int K, int w,
+                                                const double *e64)
+{
+    if (!(t > 0.0)) return -23.025850929940456840;   // log(1e-10)
+    double pdf = 0.0, surv = 1.0;
+    for (int k = 0; k < K; ++k) {
+        const double *e = e64 + 5 * ents[k];
+        const double A = e[0], b = e[1], v = e[2], s = e[3], den = e[4];
+        const double ts = __dmul_rn(t, s);
+        const double chim = __dsub_rn(b, __dmul_rn(t, v)), xx = __dsub_rn(chim, A);
+        const double cz = __ddiv_rn(chim, ts), czm = __ddiv_rn(xx, ts);
+        if (k == w) {
+            const double f = __ddiv_rn(__dadd_rn(__dmul_rn(v, __dsub_rn(Phi64(cz), Phi64(czm))),
+                                                 __dmul_rn(s, __dsub_rn(phi64(czm), phi64(cz)))), A);
+            pdf = __ddiv_rn(f, den);
+        } else {
+            const double in = __dsub_rn(__dadd_rn(__dmul_rn(ts, __dsub_rn(phi64(czm), phi64(cz))),
+                                                  __dmul_rn(xx, Phi64(czm))),
+                                        __dmul_rn(chim, Phi64(cz)));
+            const double F = __dadd_rn(1.0, __ddiv_rn(in, A));
+            surv = __dmul_rn(surv, __dsub_rn(1.0, __ddiv_rn(F, den)));
+        }
+    }
+    if (!(pdf > 1e-10)) pdf = 1e-10;
+    double d = __dmul_rn(pdf, surv);
+    if (!(d > 0.0)) d = 2.220446049250313080847e-16;
+    return log(d);
+}
+
+// ------------------------------------------------------ FP32 LBA trial
+// e32a[u] = (beta = b/s, betam = (b-A)/s, kappa = v/s, cs = s/(A Phi(v/s)))
+// e32b[u] = (cv = v/(A Phi(v/s)), q = Phi(-v/s)/Phi(v/s))
+// z = beta/t - kappa.  Winner: pdf = cv*(Phi(cz)-Phi(czm)) + cs*(phi(czm)-phi(cz)),
+// with the difference taken on the upper tail when czm >= 0.  Loser survivor:
+// late (cz < 0) t*cs*(phi(cz)-phi(czm) + cz Phi(cz) - czm Phi(czm)) - q,
+// early 1 - t*cs*(cz Q(cz) - czm Q(czm) + phi(czm) - phi(cz)).
+// Returns false when the trial must be re-evaluated in FP64: a survivor in
+// the range where either form loses digits, a pdf near the 1e-10 floor, a
+// non-positive product or t below 1e-4 s.
+__device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int K, int w,
+                                              const float4 *e32a, const float2 *e32b,
+                                              float &ld)
+{
+    if (!(t > 1e-4f)) return false;
+    const float it = __frcp_rn(t);
+    float pdf;
+    {
+        const float4 a = e32a[ents[w]];
+        const float2 b = e32b[ents[w]];
+        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
+        const float pz = phi32(cz), pm = phi32(czm);
+        const float sg = (czm >= 0.f) ? -1.f : 1.f;
+        const float d = sg * (normcdff(sg * cz) - normcdff(sg * czm));
+        pdf = fmaf(b.x, d, a.w * (pm - pz));
+    }
+    float surv = 1.f;
+    bool bad = false;
+    for (int j = 0; j < K - 1; ++j) {
+        const int k = (j < w) ? j : j + 1;
+        const float4 a = e32a[ents[k]];
+        const float2 b = e32b[ents[k]];
+        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
+        const float pz = phi32(cz), pm = phi32(czm);
+        const bool late = cz < 0.f;
+        const float sg = late ? 1.f : -1.f;
+        const float br = fmaf(cz, normcdff(sg * cz), -czm * normcdff(sg * czm)) + sg * (pz - pm);
+        const float tcs = t * a.w;
+        const float S = late ? fmaf(tcs, br, -b.y) : fmaf(-tcs, br, 1.f);
+        surv *= S;
+        // Early, S = 1 - F cancels as F -> 1; late, S1/Phi(v/s) - q cancels as
+        // S1 -> Phi(-v/s); below 1e-9 the reference's own FP64 form loses its
+        // digits (it cancels to <= 0 and takes DBL_EPSILON), so follow it there.
+        bad |= late ? !(S >= 1e-9f && S * 32.f >= b.y) : !(S >= 1e-2f);
+    }
+    const float d = pdf * surv;
+    if (bad || !(pdf >= 1e-8f) || !(d > 0.f) || !(d < 3.0e38f)) return false;
+    ld = __logf(d);
+    return true;
+}
+
+}  // namespace ggdmc

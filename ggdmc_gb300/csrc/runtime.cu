@@ -1,0 +1,1013 @@
+// runtime.cu -- host side of the C ABI in include/ggdmc_gpu.h.
+//
+// Owns device memory (a handle holds the design and the trials; a run adds
+// chain state, proposal buffers and the sample store), builds one DE
+// iteration as a launch sequence, captures a block of iterations into a CUDA
+// graph and replays it, then copies the thinned samples back into the
+// caller's arrays (R's posterior layout).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "../../include/ggdmc_gpu.h"
+#include "sampler.cuh"
+
+using namespace ggdmc;
+
+namespace {
+
+thread_local std::string g_err;
+constexpr size_t kFlushBytes = (size_t)256 << 20;   // twice the 126 MB L2
+
+ggdmc_status fail(ggdmc_status s, const std::string &msg)
+{
+    g_err = msg;
+    return s;
+}
+
+#define CU(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(GGDMC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count)
+    {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        n = count;
+        return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    }
+    cudaError_t upload(const T *h, size_t count, cudaStream_t st)
+    {
+        cudaError_t e = alloc(count);
+        if (e) return e;
+        return count ? cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st)
+                     : cudaSuccess;
+    }
+};
+
+double host_Phi(double z) { return 0.5 * std::erfc(-z * 0.70710678118654752440); }
+
+// Prior row (dist_id, p0, p1, lower, upper, c); see sampler.cuh.
+ggdmc_status prior_rows(const ggdmc_prior *p, std::vector<double> &rows)
+{
+    if (!p || p->n_par <= 0 || !p->table) return fail(GGDMC_ERR_ARG, "prior table is empty");
+    rows.assign((size_t)p->n_par * kPriorRow, 0.0);
+    for (int j = 0; j < p->n_par; ++j) {
+        const double *t = p->table + 6 * j;
+        const int id = (int)t[4];
+        if (t[5] == 0.0) return fail(GGDMC_ERR_ARG, "prior with log_p = FALSE is not supported");
+        double *o = rows.data() + kPriorRow * j;
+        o[0] = id; o[1] = t[0]; o[2] = t[1]; o[3] = t[2]; o[4] = t[3];
+        if (id == GGDMC_PRIOR_TNORM) {
+            const double mu = t[0], sg = t[1], lo = t[2], hi = t[3];
+            if (!(sg > 0.0)) {
+                o[5] = -INFINITY;
+            } else {
+                const double a = (lo - mu) / sg, b = (hi - mu) / sg;
+                double mass;
+                if (std::isinf(hi) && hi > 0) mass = 0.5 * std::erfc(a * 0.70710678118654752440);
+                else if (std::isinf(lo) && lo < 0) mass = 0.5 * std::erfc(-b * 0.70710678118654752440);
+                else mass = host_Phi(b) - host_Phi(a);
+                o[5] = -0.91893853320467274178 - std::log(sg) - std::log(mass);
+            }
+        } else if (id == GGDMC_PRIOR_UNIF) {
+            o[5] = -std::log(t[1] - t[0]);
+        } else {
+            return fail(GGDMC_ERR_ARG, "prior dist_id " + std::to_string(id) +
+                                           " is not supported (1 = tnorm, 6 = unif)");
+        }
+    }
+    return GGDMC_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ handle
+struct ggdmc_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // design
+    int model_type = 0, n_par = 0, n_cell = 0, n_acc = 0, n_ent = 0, n_const = 0;
+    DevBuf<EntSrc> ent_src;
+    DevBuf<uint8_t> cell_ent, cell_w, cell_t0;
+    DevBuf<int32_t> t0_src, ddm_src;
+    int n_t0 = 0;
+    int n_sm = 0;
+    DevBuf<double> consts;
+    // trials
+    int S = 0;
+    std::vector<int64_t> h_offs;
+    DevBuf<int64_t> offs;
+    DevBuf<double> rt64;
+    DevBuf<float2> rt32;
+    DevBuf<uint16_t> cell;
+    // run workspace
+    DevBuf<double> th, lp, ll, th_s, lp_s, ll_s, phi_tab, pp_bounds, prior, hprior, hrows;
+    DevBuf<double> pth, plp, pll, pth_s, plp_s, pll_s, pref_src, pref_next;
+    DevBuf<int32_t> partner, ptype, nstep, sub, migrated, ppartner, pptype, pnstep, psub,
+        pmigrated, iter, status, items, items_plain, rs_decided, rs_para, queue, qn, qc;
+    DevBuf<int8_t> need, pneed;
+    DevBuf<uint8_t> rs_done, rs_mod, rs_pend;
+    DevBuf<double> part;
+    DevBuf<float4> tab_a;
+    DevBuf<float2> tab_b, tab_t;
+    DevBuf<int32_t> tab_bad;
+    DevBuf<int16_t> rs_ver;
+    DevBuf<double> jit, accu, pjit, paccu;
+    DevBuf<double> smp_th, smp_lp, smp_ll, psmp_th, psmp_lp, psmp_ll, draws;
+    DevBuf<unsigned long long> stats;
+    DevBuf<double> io_a, io_b;
+    DevBuf<uint8_t> flushbuf;
+
+    DevModel dev_model() const
+    {
+        DevModel m{};
+        m.model_type = model_type;
+        m.n_par = n_par;
+        m.n_cell = n_cell;
+        m.n_acc = n_acc;
+        m.n_ent = n_ent;
+        m.n_const = n_const;
+        m.n_t0 = n_t0;
+        m.t0_src = t0_src.p;
+        m.ent_src = ent_src.p;
+        m.cell_ent = cell_ent.p;
+        m.cell_w = cell_w.p;
+        m.cell_t0 = cell_t0.p;
+        m.ddm_src = ddm_src.p;
+        m.consts = consts.p;
+        return m;
+    }
+};
+
+namespace {
+
+double timeout_seconds()
+{
+    const char *s = std::getenv("GGDMC_TIMEOUT_S");
+    double v = s ? std::atof(s) : 0.0;
+    return v > 0.0 ? v : 1800.0;
+}
+
+// Wait for all work on the stream with a deadline; never blocks forever.
+ggdmc_status wait_stream(cudaStream_t st)
+{
+    cudaEvent_t ev;
+    CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e) {
+        cudaEventDestroy(ev);
+        return fail(GGDMC_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const double lim = timeout_seconds();
+    int spins = 0;
+    for (;;) {
+        e = cudaEventQuery(ev);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) {
+            cudaEventDestroy(ev);
+            return fail(GGDMC_ERR_CUDA, std::string("device work failed: ") + cudaGetErrorString(e));
+        }
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > lim) {
+            cudaEventDestroy(ev);
+            return fail(GGDMC_ERR_TIMEOUT, "device work exceeded GGDMC_TIMEOUT_S");
+        }
+        if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    cudaEventDestroy(ev);
+    return GGDMC_OK;
+}
+
+ggdmc_status build_design(ggdmc_handle *h, const ggdmc_model *m)
+{
+    if (!m || !m->param_src || !m->resp) return fail(GGDMC_ERR_ARG, "model is NULL or incomplete");
+    if (m->model_type != GGDMC_MODEL_LBA)
+        return fail(GGDMC_ERR_ARG, "only the LBA model runs on this build");
+    if (m->n_kind != GGDMC_LBA_NKIND) return fail(GGDMC_ERR_ARG, "LBA model needs n_kind == 6");
+    if (m->n_par < 1 || m->n_par > kMaxPar) return fail(GGDMC_ERR_ARG, "n_par out of range (1..64)");
+    if (m->n_cell < 1 || m->n_cell > kMaxCell) return fail(GGDMC_ERR_ARG, "n_cell out of range");
+    if (m->n_acc < 2 || m->n_acc > kMaxAcc) return fail(GGDMC_ERR_ARG, "n_acc out of range (2..8)");
+    if (m->n_const < 0 || (m->n_const > 0 && !m->constants))
+        return fail(GGDMC_ERR_ARG, "constants missing");
+    auto check_src = [&](int32_t s) {
+        return (s >= 0 && s < m->n_par) || (s < 0 && -1 - s < m->n_const);
+    };
+    auto value_if_const = [&](int32_t s, double &v) {
+        if (s < 0) { v = m->constants[-1 - s]; return true; }
+        return false;
+    };
+    const int K = m->n_acc, NK = m->n_kind;
+    std::map<std::tuple<int, int, int, int>, int> uniq;
+    std::vector<EntSrc> ents;
+    std::vector<uint8_t> cent((size_t)m->n_cell * K), cw(m->n_cell);
+    std::vector<int32_t> ct0(m->n_cell);
+    std::vector<uint8_t> ct0i(m->n_cell);
+    std::vector<int32_t> t0s;
+    for (int c = 0; c < m->n_cell; ++c) {
+        if (m->resp[c] < 0 || m->resp[c] >= K) return fail(GGDMC_ERR_ARG, "resp index out of range");
+        cw[c] = (uint8_t)m->resp[c];
+        for (int k = 0; k < K; ++k) {
+            const int32_t *q = m->param_src + ((size_t)c * K + k) * NK;
+            for (int j = 0; j < NK; ++j)
+                if (!check_src(q[j])) return fail(GGDMC_ERR_ARG, "parameter source out of range");
+            double st0;
+            if (!value_if_const(q[5], st0) || st0 != 0.0)
+                return fail(GGDMC_ERR_ARG, "LBA with st0 other than the constant 0 is not supported");
+            if (k == 0) ct0[c] = q[4];
+            else if (q[4] != ct0[c])
+                return fail(GGDMC_ERR_ARG, "t0 must be the same for every accumulator of a cell");
+            auto key = std::make_tuple(q[0], q[1], q[2], q[3]);
+            auto it = uniq.find(key);
+            int id;
+            if (it == uniq.end()) {
+                id = (int)ents.size();
+                if (id >= kMaxEnt) return fail(GGDMC_ERR_ARG, "too many distinct accumulator tuples");
+                uniq[key] = id;
+                ents.push_back(EntSrc{q[0], q[1], q[2], q[3]});
+            } else {
+                id = it->second;
+            }
+            cent[(size_t)c * K + k] = (uint8_t)id;
+        }
+    }
+    for (int c = 0; c < m->n_cell; ++c) {
+        auto it = std::find(t0s.begin(), t0s.end(), ct0[c]);
+        if (it == t0s.end()) {
+            if ((int)t0s.size() >= kMaxT0) return fail(GGDMC_ERR_ARG, "too many distinct t0 sources");
+            t0s.push_back(ct0[c]);
+            it = t0s.end() - 1;
+        }
+        ct0i[c] = (uint8_t)(it - t0s.begin());
+    }
+    h->n_t0 = (int)t0s.size();
+    h->model_type = m->model_type;
+    h->n_par = m->n_par;
+    h->n_cell = m->n_cell;
+    h->n_acc = K;
+    h->n_ent = (int)ents.size();
+    h->n_const = m->n_const;
+    std::vector<double> consts(m->constants, m->constants + m->n_const);
+    if (consts.empty()) consts.push_back(0.0);
+    cudaStream_t st = h->stream;
+    CU(h->ent_src.upload(ents.data(), ents.size(), st));
+    CU(h->cell_ent.upload(cent.data(), cent.size(), st));
+    CU(h->cell_w.upload(cw.data(), cw.size(), st));
+    CU(h->cell_t0.upload(ct0i.data(), ct0i.size(), st));
+    CU(h->t0_src.upload(t0s.data(), t0s.size(), st));
+    CU(h->consts.upload(consts.data(), consts.size(), st));
+    CU(configure_kernels(h->dev_model()));
+    return GGDMC_OK;
+}
+
+ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
+{
+    if (!d) { h->S = 0; h->h_offs.assign(1, 0); return GGDMC_OK; }
+    if (d->n_subject < 0 || !d->offsets) return fail(GGDMC_ERR_ARG, "data is incomplete");
+    const int S = d->n_subject;
+    std::vector<int64_t> offs(d->offsets, d->offsets + S + 1);
+    if (offs[0] != 0) return fail(GGDMC_ERR_ARG, "offsets[0] must be 0");
+    for (int s = 0; s < S; ++s)
+        if (offs[s + 1] < offs[s]) return fail(GGDMC_ERR_ARG, "offsets must be non-decreasing");
+    const int64_t N = offs[S];
+    if (N > 0 && (!d->rt || !d->cell)) return fail(GGDMC_ERR_ARG, "rt / cell missing");
+    std::vector<float2> r32(N);
+    std::vector<uint16_t> c16(N);
+    for (int64_t i = 0; i < N; ++i) {
+        const double rt = d->rt[i];
+        if (!std::isfinite(rt)) return fail(GGDMC_ERR_ARG, "non-finite RT in data");
+        const int c = d->cell[i];
+        if (c < 0 || c >= h->n_cell) return fail(GGDMC_ERR_ARG, "cell index out of range");
+        const float hi = (float)rt;
+        r32[i] = make_float2(hi, (float)(rt - (double)hi));
+        c16[i] = (uint16_t)c;
+    }
+    h->S = S;
+    h->h_offs = offs;
+    cudaStream_t st = h->stream;
+    CU(h->offs.upload(offs.data(), offs.size(), st));
+    CU(h->rt64.upload(d->rt, N, st));
+    CU(h->rt32.upload(r32.data(), N, st));
+    CU(h->cell.upload(c16.data(), N, st));
+    return wait_stream(st);
+}
+
+ggdmc_status check_cfg(const ggdmc_de_config *c)
+{
+    if (!c) return fail(GGDMC_ERR_ARG, "config is NULL");
+    if (c->nchain <= 2) return fail(GGDMC_ERR_ARG, "Require three or more chains.");
+    if (c->nchain > kMaxChain) return fail(GGDMC_ERR_ARG, "nchain above 1024");
+    if (c->nmc < 1 || c->thin < 1) return fail(GGDMC_ERR_ARG, "nmc and thin must be >= 1");
+    if (c->nparameter < 1 || c->nparameter > kMaxTheta)
+        return fail(GGDMC_ERR_ARG, "nparameter out of range");
+    if (!(c->rp > 0.0) || !(c->gamma_precursor > 0.0))
+        return fail(GGDMC_ERR_ARG, "rp and gamma_precursor must be positive");
+    if (c->precision < GGDMC_FP64 || c->precision > GGDMC_FP64_PLAIN)
+        return fail(GGDMC_ERR_ARG, "unknown precision");
+    return GGDMC_OK;
+}
+
+enum RunKind { RK_SUBJECTS, RK_HIER, RK_HYPER };
+
+struct RunArgs {
+    RunKind kind;
+    const ggdmc_de_config *cfg;
+    const ggdmc_prior *p_prior, *h_prior;
+    ggdmc_chain_state *phi_state, *subj_state;
+    const double *draws;
+    ggdmc_samples *phi_out, *subj_out;
+    ggdmc_run_stats *stats;
+    const double *hyper_rows;
+    int n_row;
+};
+
+ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
+{
+    ggdmc_status s;
+    if ((s = check_cfg(a.cfg))) return s;
+    const ggdmc_de_config &c = *a.cfg;
+    const int C = c.nchain;
+    const bool hier = a.kind == RK_HIER;
+    const bool hyper = a.kind == RK_HYPER;
+    const int S = hyper ? 0 : h->S;
+    const int P = hyper ? 0 : h->n_par;
+    int Pphi = 0;
+    std::vector<double> prow, hrow, bounds;
+    if ((s = prior_rows(a.p_prior, prow))) return s;
+    if (hier || hyper) {
+        if (!a.h_prior) return fail(GGDMC_ERR_ARG, "h_prior is required");
+        if ((s = prior_rows(a.h_prior, hrow))) return s;
+        Pphi = a.h_prior->n_par;
+        if (Pphi != 2 * a.p_prior->n_par)
+            return fail(GGDMC_ERR_ARG, "h_prior must have twice the parameters of p_prior");
+        if (Pphi > kMaxTheta) return fail(GGDMC_ERR_ARG, "phi has too many parameters");
+        if (!a.phi_state) return fail(GGDMC_ERR_ARG, "phi state is required");
+        bounds.resize(2 * (size_t)a.p_prior->n_par);
+        for (int j = 0; j < a.p_prior->n_par; ++j) {
+            bounds[2 * j] = a.p_prior->table[6 * j + 2];
+            bounds[2 * j + 1] = a.p_prior->table[6 * j + 3];
+        }
+    }
+    if (!hyper) {
+        if (S < 1) return fail(GGDMC_ERR_ARG, "no subjects in the handle");
+        if (a.p_prior->n_par != P) return fail(GGDMC_ERR_ARG, "p_prior size differs from n_par");
+        if (!a.subj_state) return fail(GGDMC_ERR_ARG, "subject state is required");
+        if (!hier && c.nparameter != P)
+            return fail(GGDMC_ERR_ARG, "nparameter must equal the model's n_par");
+        if (hier && c.nparameter / 2 > P)
+            return fail(GGDMC_ERR_ARG, "nparameter/2 exceeds the subject parameters");
+    } else if (c.nparameter > Pphi) {
+        return fail(GGDMC_ERR_ARG, "nparameter exceeds the phi parameters");
+    }
+    if (hier && c.nparameter > Pphi) return fail(GGDMC_ERR_ARG, "nparameter exceeds phi length");
+
+    cudaStream_t st = h->stream;
+    const int nmc = c.nmc;
+    const int64_t n_iter = (int64_t)(nmc - 1) * c.thin;
+    const int n_level = hier ? S + 1 : (hyper ? 1 : S);
+    int64_t n_pass_draw = 1;
+    if (hier) n_pass_draw = std::max<int64_t>(c.is_hblocked ? c.nparameter : 1,
+                                              c.is_pblocked ? c.nparameter / 2 : 1);
+    else if (c.is_pblocked) n_pass_draw = c.nparameter;
+    const int64_t n_slot = GGDMC_DRAW_SLOTS(C, c.nparameter);
+
+    // ---- device buffers
+    if (S > 0) {
+        CU(h->th.alloc((size_t)S * C * P));
+        CU(h->lp.alloc((size_t)S * C));
+        CU(h->ll.alloc((size_t)S * C));
+        CU(h->th_s.alloc((size_t)S * C * P));
+        CU(h->lp_s.alloc((size_t)S * C));
+        CU(h->ll_s.alloc((size_t)S * C));
+        CU(h->partner.alloc((size_t)S * C * 2));
+        CU(h->need.alloc((size_t)S * C));
+        CU(h->ptype.alloc(S));
+        CU(h->nstep.alloc(S));
+        CU(h->sub.alloc((size_t)S * C));
+        CU(h->migrated.alloc(S));
+        CU(h->jit.alloc((size_t)S * C * P));
+        CU(h->accu.alloc((size_t)S * C));
+        CU(h->rs_decided.alloc(S));
+        CU(h->rs_para.alloc(S));
+        CU(h->rs_done.alloc(S));
+        CU(h->rs_mod.alloc((size_t)S * C));
+        CU(h->rs_ver.alloc((size_t)S * C));
+        CU(h->tab_a.alloc((size_t)S * C * h->n_ent));
+        CU(h->tab_b.alloc((size_t)S * C * h->n_ent));
+        CU(h->tab_t.alloc((size_t)S * C * h->n_t0));
+        CU(h->tab_bad.alloc((size_t)S * C));
+        CU(h->smp_th.alloc((size_t)S * nmc * C * P));
+        CU(h->smp_lp.alloc((size_t)S * nmc * C));
+        CU(h->smp_ll.alloc((size_t)S * nmc * C));
+        std::vector<double> buf((size_t)S * C * P), b1((size_t)S * C), b2((size_t)S * C);
+        for (int l = 0; l < S; ++l) {
+            const ggdmc_chain_state &cs = a.subj_state[l];
+            if (!cs.theta || !cs.lp || !cs.ll) return fail(GGDMC_ERR_ARG, "subject state incomplete");
+            std::memcpy(buf.data() + (size_t)l * C * P, cs.theta, sizeof(double) * C * P);
+            std::memcpy(b1.data() + (size_t)l * C, cs.lp, sizeof(double) * C);
+            std::memcpy(b2.data() + (size_t)l * C, cs.ll, sizeof(double) * C);
+        }
+        CU(cudaMemcpyAsync(h->th.p, buf.data(), sizeof(double) * buf.size(), cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(h->lp.p, b1.data(), sizeof(double) * b1.size(), cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(h->ll.p, b2.data(), sizeof(double) * b2.size(), cudaMemcpyHostToDevice, st));
+        { ggdmc_status ws_ = wait_stream(st); if (ws_) return ws_; }
+        // trial-count-descending work list for the likelihood kernel
+        std::vector<int> order(S);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            return (h->h_offs[x + 1] - h->h_offs[x]) > (h->h_offs[y + 1] - h->h_offs[y]);
+        });
+        std::vector<int32_t> items((size_t)S * C), plain((size_t)S * C);
+        for (int q = 0; q < S; ++q)
+            for (int k = 0; k < C; ++k) items[(size_t)q * C + k] = order[q] * C + k;
+        for (size_t q = 0; q < plain.size(); ++q) plain[q] = (int32_t)q;
+        CU(h->items.upload(items.data(), items.size(), st));
+        CU(h->items_plain.upload(plain.data(), plain.size(), st));
+    }
+    if (Pphi > 0) {
+        CU(h->pth.alloc((size_t)C * Pphi));
+        CU(h->plp.alloc(C));
+        CU(h->pll.alloc(C));
+        CU(h->pth_s.alloc((size_t)C * Pphi));
+        CU(h->plp_s.alloc(C));
+        CU(h->pll_s.alloc(C));
+        CU(h->pref_src.alloc(C));
+        CU(h->pref_next.alloc(C));
+        CU(h->ppartner.alloc((size_t)C * 2));
+        CU(h->pneed.alloc(C));
+        CU(h->pptype.alloc(1));
+        CU(h->pnstep.alloc(1));
+        CU(h->psub.alloc(C));
+        CU(h->pmigrated.alloc(1));
+        CU(h->pjit.alloc((size_t)C * Pphi));
+        CU(h->paccu.alloc(C));
+        CU(h->psmp_th.alloc((size_t)nmc * C * Pphi));
+        CU(h->psmp_lp.alloc((size_t)nmc * C));
+        CU(h->psmp_ll.alloc((size_t)nmc * C));
+        CU(h->hprior.upload(hrow.data(), hrow.size(), st));
+        CU(h->pp_bounds.upload(bounds.data(), bounds.size(), st));
+        const ggdmc_chain_state &ps = *a.phi_state;
+        if (!ps.theta || !ps.lp || !ps.ll) return fail(GGDMC_ERR_ARG, "phi state incomplete");
+        CU(cudaMemcpyAsync(h->pth.p, ps.theta, sizeof(double) * C * Pphi, cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(h->plp.p, ps.lp, sizeof(double) * C, cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(h->pll.p, ps.ll, sizeof(double) * C, cudaMemcpyHostToDevice, st));
+    }
+    if (hier) CU(h->phi_tab.alloc((size_t)C * P * 3));
+    if (!hier && !hyper) CU(h->prior.upload(prow.data(), prow.size(), st));
+    if (hyper) {
+        if (!a.hyper_rows || a.n_row < 1) return fail(GGDMC_ERR_ARG, "hyper data is empty");
+        CU(h->hrows.upload(a.hyper_rows, (size_t)a.n_row * (Pphi / 2), st));
+    }
+    const int64_t n_draw = n_iter * n_level * n_pass_draw * n_slot;
+    if (a.draws) CU(h->draws.upload(a.draws, (size_t)n_draw, st));
+    const bool plain = c.precision == GGDMC_FP64_PLAIN;
+    int n_round = 0;
+    if (const char *rs = std::getenv("GGDMC_ROUNDS")) n_round = std::max(0, std::atoi(rs));
+    if (plain || S == 0) n_round = 0;
+    int chunk = 256;
+    if (const char *cs = std::getenv("GGDMC_CHUNK")) chunk = std::max(32, std::atoi(cs));
+    int64_t max_n = 0;
+    for (int l = 0; l < S; ++l) max_n = std::max<int64_t>(max_n, h->h_offs[l + 1] - h->h_offs[l]);
+    const int max_chunk = (int)std::max<int64_t>(1, (max_n + chunk - 1) / chunk);
+    CU(h->qn.alloc(std::max(n_round, 1)));
+    CU(h->qc.alloc(std::max(n_round, 1)));
+    CU(h->queue.alloc((size_t)std::max(n_round, 1) * std::max(S, 1) * C * max_chunk));
+    CU(h->part.alloc((size_t)std::max(S, 1) * C * max_chunk));
+    CU(h->rs_pend.alloc((size_t)std::max(S, 1) * C));
+    CU(h->iter.alloc(1));
+    CU(h->status.alloc(1));
+    CU(h->stats.alloc(ST_N));
+    CU(cudaMemsetAsync(h->stats.p, 0, sizeof(unsigned long long) * ST_N, st));
+    CU(cudaMemsetAsync(h->iter.p, 0, sizeof(int32_t), st));
+    CU(cudaMemsetAsync(h->status.p, 0, sizeof(int32_t), st));
+
+    // ---- run description
+    RunDev r{};
+    r.C = C; r.P = P; r.Pphi = Pphi; r.S = S;
+    r.Pn = c.nparameter; r.half = c.nparameter / 2;
+    r.loop = hier ? LOOP_HCHAINS : LOOP_CHAINS;
+    r.level0 = hier ? 1 : 0;
+    r.prec = (c.precision == GGDMC_MIXED) ? PREC_MIXED : PREC_FP64;
+    r.sub_blocked = c.is_pblocked;
+    r.phi_blocked = hier ? c.is_hblocked : c.is_pblocked;
+    r.phi_loop = hier ? LOOP_HCHAINS : LOOP_CHAINS;
+    r.thin = c.thin; r.nmc = nmc;
+    r.gamma = c.gamma_precursor / std::sqrt(2.0 * c.nparameter);
+    r.rp = c.rp; r.sub_mig = c.sub_migration_prob; r.pop_mig = c.pop_migration_prob;
+    r.ds.draws = a.draws ? h->draws.p : nullptr;
+    r.ds.seed = c.seed;
+    r.ds.n_level = n_level; r.ds.n_pass = n_pass_draw; r.ds.n_slot = n_slot;
+    r.iter = h->iter.p;
+    r.m = h->dev_model();
+    r.offs = h->offs.p; r.rt64 = h->rt64.p; r.rt32 = h->rt32.p; r.cell = h->cell.p;
+    r.th = h->th.p; r.lp = h->lp.p; r.ll = h->ll.p;
+    r.th_s = h->th_s.p; r.lp_s = h->lp_s.p; r.ll_s = h->ll_s.p;
+    r.partner = h->partner.p; r.need = h->need.p; r.ptype = h->ptype.p; r.nstep = h->nstep.p;
+    r.sub = h->sub.p; r.migrated = h->migrated.p;
+    r.jit = h->jit.p; r.accu = h->accu.p;
+    r.tab_a = h->tab_a.p; r.tab_b = h->tab_b.p; r.tab_t = h->tab_t.p; r.tab_bad = h->tab_bad.p;
+    r.rs_decided = h->rs_decided.p; r.rs_para = h->rs_para.p; r.rs_done = h->rs_done.p;
+    r.rs_mod = h->rs_mod.p; r.rs_ver = h->rs_ver.p;
+    r.queue = h->queue.p; r.qn = h->qn.p; r.qc = h->qc.p; r.n_round = n_round;
+    r.part = h->part.p; r.rs_pend = h->rs_pend.p; r.chunk = chunk; r.max_chunk = max_chunk;
+    r.pjit = h->pjit.p; r.paccu = h->paccu.p;
+    r.prior = (!hier && !hyper) ? h->prior.p : nullptr;
+    r.pp_bounds = (hier || hyper) ? h->pp_bounds.p : nullptr;
+    r.phi_tab = hier ? h->phi_tab.p : nullptr;
+    r.pth = h->pth.p; r.plp = h->plp.p; r.pll = h->pll.p;
+    r.pth_s = h->pth_s.p; r.plp_s = h->plp_s.p; r.pll_s = h->pll_s.p;
+    r.pref_src = h->pref_src.p; r.pref_next = h->pref_next.p;
+    r.ppartner = h->ppartner.p; r.pneed = h->pneed.p; r.pptype = h->pptype.p;
+    r.pnstep = h->pnstep.p; r.psub = h->psub.p; r.pmigrated = h->pmigrated.p;
+    r.hprior = (hier || hyper) ? h->hprior.p : nullptr;
+    r.hrows = hyper ? h->hrows.p : nullptr;
+    r.n_row = hyper ? a.n_row : 0;
+    r.smp_th = h->smp_th.p; r.smp_lp = h->smp_lp.p; r.smp_ll = h->smp_ll.p;
+    r.psmp_th = h->psmp_th.p; r.psmp_lp = h->psmp_lp.p; r.psmp_ll = h->psmp_ll.p;
+    r.stats = h->stats.p;
+    r.status = h->status.p;
+
+    int64_t launches_per_iter = 0;
+    const int queue_blocks = h->n_sm * 8;
+    // One DE iteration (src/de.cpp:201-242 / 272-383) as a launch sequence.
+    auto one_iteration = [&]() -> cudaError_t {
+        cudaError_t e;
+        if (Pphi > 0) {
+            const int npass = hier ? (c.is_hblocked ? c.nparameter : 1)
+                                   : (c.is_pblocked ? c.nparameter : 1);
+            for (int p = 0; p < npass; ++p) {
+                if ((e = launch_phi_propose(r, p, st))) return e;
+                if ((e = launch_phi_eval(r, st))) return e;
+                if ((e = launch_phi_resolve(r, p, st))) return e;
+                launches_per_iter += 3;
+            }
+            if (hier) {
+                if ((e = launch_phi_tables(r, st))) return e;
+                ++launches_per_iter;
+            }
+        }
+        if (S > 0) {
+            const int npass = hier ? (c.is_pblocked ? c.nparameter / 2 : 1)
+                                   : (c.is_pblocked ? c.nparameter : 1);
+            for (int p = 0; p < npass; ++p) {
+                if ((e = launch_sub_propose(r, p, st))) return e;
+                ++launches_per_iter;
+                if (plain) {
+                    for (int l = 0; l < S; ++l) {
+                        if ((e = launch_sub_loglik(r, h->items_plain.p + (size_t)l * C, C, st))) return e;
+                        if ((e = launch_sub_resolve(r, p, l, 1, st))) return e;
+                        launches_per_iter += 2;
+                    }
+                } else {
+                    if ((e = launch_sub_loglik(r, h->items.p, S * C, st))) return e;
+                    for (int rd = 0; rd < n_round; ++rd) {
+                        if ((e = launch_sub_round(r, p, rd, st))) return e;
+                        if ((e = launch_sub_loglik_queue(r, rd, queue_blocks, st))) return e;
+                    }
+                    if ((e = launch_sub_resolve(r, p, 0, S, st))) return e;
+                    launches_per_iter += 2 + 2 * n_round;
+                }
+            }
+        }
+        if ((e = launch_store(r, st))) return e;
+        if ((e = launch_next_iter(r, st))) return e;
+        launches_per_iter += 2;
+        return cudaSuccess;
+    };
+
+    // slot 0 = start state, then iterations 1..n_iter
+    CU(launch_store(r, st));
+    CU(launch_next_iter(r, st));
+    int64_t launches = 2;
+    double sweep_ms = 0.0;
+    // cfg->flags bit 0: flush L2 (a memset larger than L2) between
+    // iterations and time only the iterations' kernels, by event nodes.
+    const bool flush = (c.flags & GGDMC_FLAG_L2_FLUSH) != 0;
+    if (n_iter > 0) {
+        const char *gs = std::getenv("GGDMC_GRAPH_ITERS");
+        int64_t per_graph = gs ? std::max(1, std::atoi(gs)) : 8;
+        per_graph = std::min<int64_t>(per_graph, n_iter);
+        if (flush) CU(h->flushbuf.alloc(kFlushBytes));
+        std::vector<cudaEvent_t> ev_a(per_graph + 1), ev_b(per_graph + 1);
+        for (auto &e : ev_a) CU(cudaEventCreate(&e));
+        for (auto &e : ev_b) CU(cudaEventCreate(&e));
+        auto cleanup_events = [&]() {
+            for (auto &e : ev_a) cudaEventDestroy(e);
+            for (auto &e : ev_b) cudaEventDestroy(e);
+        };
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaSuccess;
+        launches_per_iter = 0;
+        for (int64_t i = 0; i < per_graph && ce == cudaSuccess; ++i) {
+            // external event nodes: recorded (and timeable) on every replay
+            if (flush) ce = cudaEventRecordWithFlags(ev_a[i], st, cudaEventRecordExternal);
+            if (!ce) ce = one_iteration();
+            if (flush && !ce) ce = cudaEventRecordWithFlags(ev_b[i], st, cudaEventRecordExternal);
+            if (flush && !ce) ce = cudaMemsetAsync(h->flushbuf.p, (int)(i & 0xff), kFlushBytes, st);
+        }
+        cudaError_t ee = cudaStreamEndCapture(st, &graph);
+        if (ce || ee) {
+            cleanup_events();
+            if (graph) cudaGraphDestroy(graph);
+            return fail(GGDMC_ERR_CUDA, std::string("graph capture: ") +
+                                            cudaGetErrorString(ce ? ce : ee));
+        }
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        if (ie) {
+            cleanup_events();
+            cudaGraphDestroy(graph);
+            return fail(GGDMC_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+        }
+        const int64_t per_iter = launches_per_iter / per_graph;
+        int64_t done = 0;
+        ggdmc_status ws = GGDMC_OK;
+        if (!flush) CU(cudaEventRecord(ev_a[per_graph], st));
+        while (done + per_graph <= n_iter && !ws) {
+            cudaError_t e = cudaGraphLaunch(exec, st);
+            if (e) {
+                ws = fail(GGDMC_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+                break;
+            }
+            done += per_graph;
+            if (!flush) continue;
+            // read this replay's event nodes before the next replay reuses them
+            ws = wait_stream(st);
+            if (ws) break;
+            for (int64_t i = 0; i < per_graph && !ws; ++i) {
+                float ms = 0.f;
+                cudaError_t te = cudaEventElapsedTime(&ms, ev_a[i], ev_b[i]);
+                if (te) ws = fail(GGDMC_ERR_CUDA, std::string("cudaEventElapsedTime: ") +
+                                                      cudaGetErrorString(te));
+                sweep_ms += ms;
+            }
+        }
+        if (!flush && !ws) {
+            CU(cudaEventRecord(ev_b[per_graph], st));
+            ws = wait_stream(st);
+            float ms = 0.f;
+            if (!ws) cudaEventElapsedTime(&ms, ev_a[per_graph], ev_b[per_graph]);
+            sweep_ms += ms;
+        }
+        for (; done < n_iter && !ws; ++done) {
+            launches_per_iter = 0;
+            cudaError_t e = cudaEventRecord(ev_a[per_graph], st);
+            if (!e) e = one_iteration();
+            if (!e) e = cudaEventRecord(ev_b[per_graph], st);
+            if (e) {
+                ws = fail(GGDMC_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+                break;
+            }
+            ws = wait_stream(st);
+            float ms = 0.f;
+            if (!ws) cudaEventElapsedTime(&ms, ev_a[per_graph], ev_b[per_graph]);
+            sweep_ms += ms;
+            if (flush && !ws) cudaMemsetAsync(h->flushbuf.p, 0, kFlushBytes, st);
+        }
+        launches += n_iter * per_iter;
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        cleanup_events();
+        if (ws) return ws;
+    }
+
+    // ---- copy back: final state and samples
+    if (S > 0) {
+        std::vector<double> buf((size_t)S * C * P), b1((size_t)S * C), b2((size_t)S * C);
+        CU(cudaMemcpyAsync(buf.data(), h->th.p, sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(b1.data(), h->lp.p, sizeof(double) * b1.size(), cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(b2.data(), h->ll.p, sizeof(double) * b2.size(), cudaMemcpyDeviceToHost, st));
+        { ggdmc_status ws_ = wait_stream(st); if (ws_) return ws_; }
+        for (int l = 0; l < S; ++l) {
+            const ggdmc_chain_state &cs = a.subj_state[l];
+            std::memcpy(cs.theta, buf.data() + (size_t)l * C * P, sizeof(double) * C * P);
+            std::memcpy(cs.lp, b1.data() + (size_t)l * C, sizeof(double) * C);
+            std::memcpy(cs.ll, b2.data() + (size_t)l * C, sizeof(double) * C);
+            if (a.subj_out) {
+                const ggdmc_samples &o = a.subj_out[l];
+                if (o.theta)
+                    CU(cudaMemcpyAsync(o.theta, h->smp_th.p + (size_t)l * nmc * C * P,
+                                       sizeof(double) * nmc * C * P, cudaMemcpyDeviceToHost, st));
+                if (o.lp)
+                    CU(cudaMemcpyAsync(o.lp, h->smp_lp.p + (size_t)l * nmc * C,
+                                       sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+                if (o.ll)
+                    CU(cudaMemcpyAsync(o.ll, h->smp_ll.p + (size_t)l * nmc * C,
+                                       sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+            }
+        }
+    }
+    if (Pphi > 0) {
+        const ggdmc_chain_state &ps = *a.phi_state;
+        CU(cudaMemcpyAsync(ps.theta, h->pth.p, sizeof(double) * C * Pphi, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(ps.lp, h->plp.p, sizeof(double) * C, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(ps.ll, h->pll.p, sizeof(double) * C, cudaMemcpyDeviceToHost, st));
+        if (a.phi_out) {
+            const ggdmc_samples &o = *a.phi_out;
+            if (o.theta)
+                CU(cudaMemcpyAsync(o.theta, h->psmp_th.p, sizeof(double) * nmc * C * Pphi,
+                                   cudaMemcpyDeviceToHost, st));
+            if (o.lp)
+                CU(cudaMemcpyAsync(o.lp, h->psmp_lp.p, sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+            if (o.ll)
+                CU(cudaMemcpyAsync(o.ll, h->psmp_ll.p, sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    unsigned long long hs[ST_N];
+    CU(cudaMemcpyAsync(hs, h->stats.p, sizeof hs, cudaMemcpyDeviceToHost, st));
+    if ((s = wait_stream(st))) return s;
+    if (a.stats) {
+        a.stats->proposals = (int64_t)hs[ST_PROPOSALS];
+        a.stats->accepts = (int64_t)hs[ST_ACCEPTS];
+        a.stats->migrations = (int64_t)hs[ST_MIGRATIONS];
+        a.stats->reevaluations = (int64_t)hs[ST_REEVALS];
+        a.stats->kernel_launches = launches;
+        a.stats->trial_evals = (int64_t)hs[ST_TRIALS];
+        a.stats->resolve_rounds = (int64_t)hs[ST_ROUNDS];
+        a.stats->resolve_finish = (int64_t)hs[ST_FINISH];
+        a.stats->iterations = n_iter;
+        a.stats->sweep_ms = sweep_ms;
+    }
+    return GGDMC_OK;
+}
+
+ggdmc_status make_handle(const ggdmc_model *model, const ggdmc_data *data, ggdmc_handle **out)
+{
+    if (!out) return fail(GGDMC_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1)
+        return fail(GGDMC_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    auto *h = new ggdmc_handle();
+    cudaGetDevice(&h->device);
+    cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
+    if (h->n_sm < 1) h->n_sm = 1;
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) {
+        delete h;
+        return fail(GGDMC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    ggdmc_status s = GGDMC_OK;
+    if (model) s = build_design(h, model);
+    if (!s) s = upload_data(h, data);
+    if (s) {
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return s;
+    }
+    *out = h;
+    return GGDMC_OK;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+const char *ggdmc_last_error(void) { return g_err.c_str(); }
+
+const char *ggdmc_version(void) { return "ggdmc_gb300 0.1 (sm_103a)"; }
+
+ggdmc_status ggdmc_draw_layout(const ggdmc_de_config *cfg, int32_t n_level, int32_t hierarchical,
+                               int64_t *n_iter, int64_t *n_pass, int64_t *n_slot, int64_t *total)
+{
+    ggdmc_status s = check_cfg(cfg);
+    if (s) return s;
+    int64_t np = 1;
+    if (hierarchical)
+        np = std::max<int64_t>(cfg->is_hblocked ? cfg->nparameter : 1,
+                               cfg->is_pblocked ? cfg->nparameter / 2 : 1);
+    else if (cfg->is_pblocked)
+        np = cfg->nparameter;
+    const int64_t ni = (int64_t)(cfg->nmc - 1) * cfg->thin;
+    const int64_t ns = GGDMC_DRAW_SLOTS(cfg->nchain, cfg->nparameter);
+    if (n_iter) *n_iter = ni;
+    if (n_pass) *n_pass = np;
+    if (n_slot) *n_slot = ns;
+    if (total) *total = ni * n_level * np * ns;
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_create(const ggdmc_model *model, const ggdmc_data *data, ggdmc_handle **out)
+{
+    if (!model) return fail(GGDMC_ERR_ARG, "model is NULL");
+    return make_handle(model, data, out);
+}
+
+ggdmc_status ggdmc_destroy(ggdmc_handle *h)
+{
+    if (!h) return GGDMC_OK;
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg, const ggdmc_prior *p_prior,
+                              const ggdmc_prior *h_prior, ggdmc_chain_state *phi_state,
+                              ggdmc_chain_state *subj_state, const double *draws,
+                              ggdmc_samples *phi_out, ggdmc_samples *subj_out, ggdmc_run_stats *stats)
+{
+    if (!h) return fail(GGDMC_ERR_ARG, "handle is NULL");
+    RunArgs a{phi_state ? RK_HIER : RK_SUBJECTS, cfg, p_prior, h_prior, phi_state, subj_state,
+              draws, phi_out, subj_out, stats, nullptr, 0};
+    return run_impl(h, a);
+}
+
+ggdmc_status ggdmc_run_subjects(const ggdmc_de_config *cfg, const ggdmc_model *model,
+                                const ggdmc_data *data, const ggdmc_prior *p_prior,
+                                ggdmc_chain_state *state, const double *draws, ggdmc_samples *out,
+                                ggdmc_run_stats *stats)
+{
+    ggdmc_handle *h = nullptr;
+    ggdmc_status s = make_handle(model, data, &h);
+    if (s) return s;
+    RunArgs a{RK_SUBJECTS, cfg, p_prior, nullptr, nullptr, state, draws, nullptr, out, stats,
+              nullptr, 0};
+    s = run_impl(h, a);
+    const std::string keep = g_err;
+    ggdmc_destroy(h);
+    g_err = keep;
+    return s;
+}
+
+ggdmc_status ggdmc_run_subject(const ggdmc_de_config *cfg, const ggdmc_model *model,
+                               const ggdmc_data *data, const ggdmc_prior *p_prior,
+                               ggdmc_chain_state *state, const double *draws, ggdmc_samples *out,
+                               ggdmc_run_stats *stats)
+{
+    if (!data || data->n_subject != 1)
+        return fail(GGDMC_ERR_ARG, "run_subject takes exactly one subject");
+    return ggdmc_run_subjects(cfg, model, data, p_prior, state, draws, out, stats);
+}
+
+ggdmc_status ggdmc_run(const ggdmc_de_config *cfg, const ggdmc_model *model, const ggdmc_data *data,
+                       const ggdmc_prior *p_prior, const ggdmc_prior *h_prior,
+                       ggdmc_chain_state *phi_state, ggdmc_chain_state *subj_state,
+                       const double *draws, ggdmc_samples *phi_out, ggdmc_samples *subj_out,
+                       ggdmc_run_stats *stats)
+{
+    ggdmc_handle *h = nullptr;
+    ggdmc_status s = make_handle(model, data, &h);
+    if (s) return s;
+    RunArgs a{RK_HIER, cfg, p_prior, h_prior, phi_state, subj_state, draws, phi_out, subj_out,
+              stats, nullptr, 0};
+    s = run_impl(h, a);
+    const std::string keep = g_err;
+    ggdmc_destroy(h);
+    g_err = keep;
+    return s;
+}
+
+ggdmc_status ggdmc_run_hyper(const ggdmc_de_config *cfg, const double *hyper_data, int32_t n_row,
+                             const ggdmc_prior *p_prior, const ggdmc_prior *h_prior,
+                             ggdmc_chain_state *state, const double *draws, ggdmc_samples *out,
+                             ggdmc_run_stats *stats)
+{
+    ggdmc_handle *h = nullptr;
+    ggdmc_status s = make_handle(nullptr, nullptr, &h);
+    if (s) return s;
+    RunArgs a{RK_HYPER, cfg, p_prior, h_prior, state, nullptr, draws, out, nullptr, stats,
+              hyper_data, n_row};
+    s = run_impl(h, a);
+    const std::string keep = g_err;
+    ggdmc_destroy(h);
+    g_err = keep;
+    return s;
+}
+
+static RunDev loglik_desc(ggdmc_handle *h, int prec)
+{
+    RunDev r{};
+    r.P = h->n_par;
+    r.S = h->S;
+    r.prec = (prec == GGDMC_MIXED) ? PREC_MIXED : PREC_FP64;
+    r.m = h->dev_model();
+    r.offs = h->offs.p; r.rt64 = h->rt64.p; r.rt32 = h->rt32.p; r.cell = h->cell.p;
+    return r;
+}
+
+ggdmc_status ggdmc_loglik_device(ggdmc_handle *h, const double *d_theta, int32_t n_theta,
+                                 int32_t precision, double *d_out, void *stream)
+{
+    if (!h || !d_theta || !d_out || n_theta < 1) return fail(GGDMC_ERR_ARG, "bad loglik arguments");
+    if (h->S < 1) return fail(GGDMC_ERR_ARG, "handle has no subjects");
+    RunDev r = loglik_desc(h, precision);
+    CU(launch_loglik_batch(r, d_theta, n_theta, d_out, (cudaStream_t)stream));
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta, int32_t precision,
+                          double *out)
+{
+    if (!h || !theta || !out || n_theta < 1) return fail(GGDMC_ERR_ARG, "bad loglik arguments");
+    if (h->S < 1) return fail(GGDMC_ERR_ARG, "handle has no subjects");
+    const size_t nt = (size_t)h->S * n_theta;
+    CU(h->io_a.upload(theta, nt * h->n_par, h->stream));
+    CU(h->io_b.alloc(nt));
+    RunDev r = loglik_desc(h, precision);
+    CU(launch_loglik_batch(r, h->io_a.p, n_theta, h->io_b.p, h->stream));
+    CU(cudaMemcpyAsync(out, h->io_b.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, h->stream));
+    return wait_stream(h->stream);
+}
+
+ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta, int32_t precision, double *out)
+{
+    if (!h || !theta || !out) return fail(GGDMC_ERR_ARG, "bad trial_logdens arguments");
+    if (h->S < 1) return fail(GGDMC_ERR_ARG, "handle has no subjects");
+    const size_t N = (size_t)h->h_offs[h->S];
+    CU(h->io_a.upload(theta, (size_t)h->S * h->n_par, h->stream));
+    CU(h->io_b.alloc(std::max<size_t>(N, 1)));
+    RunDev r = loglik_desc(h, precision);
+    CU(launch_trial_logdens(r, h->io_a.p, h->io_b.p, h->stream));
+    if (N) CU(cudaMemcpyAsync(out, h->io_b.p, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+    return wait_stream(h->stream);
+}
+
+ggdmc_status ggdmc_logprior(const ggdmc_prior *prior, const double *theta, int32_t n, double *out)
+{
+    if (!theta || !out || n < 1) return fail(GGDMC_ERR_ARG, "bad logprior arguments");
+    std::vector<double> rows;
+    ggdmc_status s = prior_rows(prior, rows);
+    if (s) return s;
+    const int P = prior->n_par;
+    double *d_rows = nullptr, *d_th = nullptr, *d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_rows, sizeof(double) * rows.size());
+    if (!e) e = cudaMalloc(&d_th, sizeof(double) * (size_t)n * P);
+    if (!e) e = cudaMalloc(&d_out, sizeof(double) * n);
+    if (!e) e = cudaMemcpy(d_rows, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_th, theta, sizeof(double) * (size_t)n * P, cudaMemcpyHostToDevice);
+    if (!e) e = launch_logprior(d_rows, P, d_th, n, d_out, nullptr);
+    if (!e) e = cudaMemcpy(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d_rows);
+    cudaFree(d_th);
+    cudaFree(d_out);
+    if (e) return fail(GGDMC_ERR_CUDA, std::string("logprior: ") + cudaGetErrorString(e));
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_loghlike(const ggdmc_prior *p_prior, const double *phi, const double *subj_theta,
+                            int32_t n_subject, int32_t n, double *out)
+{
+    if (!p_prior || !phi || !subj_theta || !out || n < 1 || n_subject < 1)
+        return fail(GGDMC_ERR_ARG, "bad loghlike arguments");
+    const int P = p_prior->n_par;
+    if (2 * P > kMaxTheta) return fail(GGDMC_ERR_ARG, "too many parameters");
+    std::vector<double> bounds(2 * (size_t)P);
+    for (int j = 0; j < P; ++j) {
+        bounds[2 * j] = p_prior->table[6 * j + 2];
+        bounds[2 * j + 1] = p_prior->table[6 * j + 3];
+    }
+    double *d_b = nullptr, *d_phi = nullptr, *d_th = nullptr, *d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_b, sizeof(double) * bounds.size());
+    if (!e) e = cudaMalloc(&d_phi, sizeof(double) * (size_t)n * 2 * P);
+    if (!e) e = cudaMalloc(&d_th, sizeof(double) * (size_t)n_subject * n * P);
+    if (!e) e = cudaMalloc(&d_out, sizeof(double) * n);
+    if (!e) e = cudaMemcpy(d_b, bounds.data(), sizeof(double) * bounds.size(), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_phi, phi, sizeof(double) * (size_t)n * 2 * P, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_th, subj_theta, sizeof(double) * (size_t)n_subject * n * P,
+                           cudaMemcpyHostToDevice);
+    if (!e) {
+        RunDev r{};
+        r.C = n; r.P = P; r.Pphi = 2 * P; r.S = n_subject;
+        r.th = d_th; r.pp_bounds = d_b;
+        e = launch_loghlike(r, d_phi, d_out, nullptr);
+    }
+    if (!e) e = cudaMemcpy(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d_b);
+    cudaFree(d_phi);
+    cudaFree(d_th);
+    cudaFree(d_out);
+    if (e) return fail(GGDMC_ERR_CUDA, std::string("loghlike: ") + cudaGetErrorString(e));
+    return GGDMC_OK;
+}
+
+}  // extern "C"

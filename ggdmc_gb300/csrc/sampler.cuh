@@ -1,0 +1,132 @@
+// sampler.cuh -- device-side run description shared by the kernels and the
+// host runtime.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "model_tables.h"
+
+namespace ggdmc {
+
+enum PassType : int32_t { PASS_CROSS = 0, PASS_MIG = 1, PASS_SKIP = 2 };
+enum Prec : int32_t { PREC_FP64 = 0, PREC_MIXED = 1 };
+// Which de.cpp loop the levels follow.
+enum LoopKind : int32_t {
+    LOOP_CHAINS = 0,   // run_chains (src/de.cpp:201-242): one selector per iteration
+    LOOP_HCHAINS = 1   // run_hchains (src/de.cpp:272-383): a selector per pass
+};
+
+// Prior row: (dist_id, p0, p1, lower, upper, c) with c the constant part of
+// the log density (truncated normal: -log(sqrt(2 pi)) - log(p1) - log(mass);
+// uniform: -log(p1 - p0)).
+constexpr int kPriorRow = 6;
+
+enum StatIdx { ST_PROPOSALS = 0, ST_ACCEPTS, ST_MIGRATIONS, ST_REEVALS, ST_TRIALS, ST_ROUNDS,
+               ST_FINISH, ST_N };
+
+struct RunDev {
+    // ------------------------------------------------------------ shape
+    int32_t C;            // chains
+    int32_t P;            // subject-level theta length
+    int32_t Pphi;         // phi-level theta length (0: no phi level)
+    int32_t S;            // subject levels
+    int32_t Pn;           // de_input nparameter (gamma, loop bound, draw stride)
+    int32_t half;         // Pn / 2
+    int32_t loop;         // LoopKind of the subject levels
+    int32_t level0;       // draw level of subject level 0
+    int32_t prec;         // Prec
+    int32_t sub_blocked;  // is_pblocked
+    int32_t phi_blocked;  // is_hblocked (phi of run) / is_pblocked (run_hyper)
+    int32_t phi_loop;     // LoopKind of the phi level
+    int32_t thin, nmc;
+    double gamma, rp, sub_mig, pop_mig;
+    DrawSrc ds;
+    int32_t *iter;        // current iteration (device counter)
+
+    // ------------------------------------------------------------ data
+    DevModel m;
+    const int64_t *offs;     // [S+1]
+    const double *rt64;      // [N]
+    const float2 *rt32;      // [N] (hi, lo)
+    const uint16_t *cell;    // [N]
+
+    // ----------------------------------------------------- subject levels
+    double *th, *lp, *ll;          // [S][C][P], [S][C]
+    double *th_s, *lp_s, *ll_s;    // proposals by step
+    int32_t *partner;              // [S][C][2]
+    int8_t *need;                  // [S][C]
+    int32_t *ptype;                // [S]
+    int32_t *nstep;                // [S]
+    int32_t *sub;                  // [S][C]
+    int32_t *migrated;             // [S] (LOOP_CHAINS: migration taken this iteration)
+    double *jit;                   // [S][C][P] jitter draws of the pass (re-proposals reuse them)
+    double *accu;                  // [S][C]    Metropolis accept uniforms of the pass
+    // ordered-decision state of a pass, kept across the global rounds
+    int32_t *rs_decided;           // [S] next step to decide
+    int32_t *rs_para;              // [S] blocked parameter of the pass, -1 for all
+    uint8_t *rs_done;              // [S]
+    uint8_t *rs_mod;               // [S][C] crossover: chain moved; migration: step accepted
+    int16_t *rs_ver;               // [S][C] decided prefix a proposal was built against
+    int32_t *queue;                // [n_round][S*C] (level*C + step) items to evaluate
+    int32_t *qn, *qc;              // [n_round] work units pushed / claimed
+    int32_t n_round;
+    double *part;                  // [S*C][max_chunk] partial sums of queued re-evaluations
+    // FP32 tables of every proposal, built where the proposal is built
+    float4 *tab_a;                 // [S*C][n_ent] (b/s, (b-A)/s, v/s, s/(A Phi(v/s)))
+    float2 *tab_b;                 // [S*C][n_ent] (v/(A Phi(v/s)), Phi(-v/s)/Phi(v/s))
+    float2 *tab_t;                 // [S*C][n_t0]  t0 as (hi, lo)
+    int32_t *tab_bad;              // [S*C] 1: outside the FP32 form's domain
+    uint8_t *rs_pend;              // [S][C] re-evaluation whose partials await summation
+    int32_t chunk;                 // trials per work unit of the queue
+    int32_t max_chunk;             // chunks of the longest subject
+    const double *prior;           // [P][kPriorRow] fixed subject prior (nullptr in HB)
+    const double *pp_bounds;       // [P][2] p_prior (lower, upper) for HB / phi level
+    double *phi_tab;               // [C][P][3] (mu, 1/sigma, c) of phi chain (HB)
+
+    // ---------------------------------------------------------- phi level
+    double *pth, *plp, *pll;       // [C][Pphi], [C]
+    double *pth_s, *plp_s, *pll_s; // proposals
+    double *pref_src, *pref_next;  // refreshed hyper log-likelihoods by step
+    int32_t *ppartner;             // [C][2]
+    int8_t *pneed;                 // [C]
+    int32_t *pptype, *pnstep, *psub, *pmigrated;
+    double *pjit, *paccu;          // [C][Pphi], [C]
+    const double *hprior;          // [Pphi][kPriorRow]
+    const double *hrows;           // run_hyper data [n_row][Pphi/2] (nullptr in HB)
+    int32_t n_row;
+
+    // ---------------------------------------------------------- samples
+    double *smp_th, *smp_lp, *smp_ll;     // [S][nmc][C][P], [S][nmc][C]
+    double *psmp_th, *psmp_lp, *psmp_ll;  // [nmc][C][Pphi], [nmc][C]
+
+    unsigned long long *stats;     // [ST_N]
+    int32_t *status;
+};
+
+// --------------------------------------------------------------- launchers
+// (defined in sampler_kernels.cu)
+cudaError_t launch_sub_propose(const RunDev &r, int pass, cudaStream_t st);
+cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, cudaStream_t st);
+cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
+                               cudaStream_t st);
+cudaError_t launch_sub_round(const RunDev &r, int pass, int round, cudaStream_t st);
+cudaError_t launch_sub_loglik_queue(const RunDev &r, int round, int n_blocks, cudaStream_t st);
+cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st);
+cudaError_t launch_phi_propose(const RunDev &r, int pass, cudaStream_t st);
+cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st);
+cudaError_t launch_phi_resolve(const RunDev &r, int pass, cudaStream_t st);
+cudaError_t launch_store(const RunDev &r, cudaStream_t st);
+cudaError_t launch_next_iter(const RunDev &r, cudaStream_t st);
+cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_theta, double *out,
+                                cudaStream_t st);
+cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *out,
+                                 cudaStream_t st);
+cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
+                            cudaStream_t st);
+cudaError_t launch_loghlike(const RunDev &r, const double *phi, double *out, cudaStream_t st);
+__host__ __device__ size_t sub_smem_bytes(const DevModel &m);
+cudaError_t configure_kernels(const DevModel &m);
+
+}  // namespace ggdmc

@@ -1,0 +1,1473 @@
+// sampler_kernels.cu -- DE-MCMC kernels for GB300 (sm_103a).
+//
+// One DE iteration of ggdmc's sampler (src/de.cpp) is a short launch
+// sequence, captured into a CUDA graph by the host runtime:
+//
+//   phi level:  k_phi_propose -> k_phi_eval -> k_phi_resolve -> k_phi_tables
+//   subjects:   k_sub_propose -> k_sub_loglik
+//               -> [k_sub_round -> k_sub_loglik_queue] x n_round
+//               -> k_sub_resolve                              (per pass)
+//   k_store -> k_next_iter
+//
+// The reference updates chains in place and in order (src/de.cpp:111-155):
+// chain i's partners may already have moved earlier in the same sweep.  The
+// kernels keep exactly that semantics by speculation.  k_sub_propose builds
+// every chain's proposal from the start-of-pass state and k_sub_loglik
+// evaluates all of them at once (the hot path: one CTA per (subject, chain),
+// trials striped over its threads).  Each k_sub_round then walks every
+// subject's chains in order, taking Metropolis decisions from the
+// speculative results for as long as a proposal is still the one the
+// sequential algorithm would have built; every chain made stale by an
+// accepted partner is re-proposed from the current state and queued, and
+// k_sub_loglik_queue evaluates the queue across the whole GPU.  k_sub_resolve
+// finishes, within one CTA per subject, what the rounds left.  Given the
+// same draws, the accepted states equal the sequential sampler's.
+#include <cfloat>
+#include <cstdio>
+#include <cstdint>
+
+#include "sampler.cuh"
+
+namespace ggdmc {
+
+constexpr int kLikThreads = 128;
+constexpr int kResolveThreads = 256;
+constexpr int kRoundThreads = 64;
+constexpr int kPhiThreads = 256;
+constexpr int kProposeThreads = 128;
+
+// ------------------------------------------------------------- helpers
+__device__ __forceinline__ double block_sum(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = (lane < nw) ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[32] = v;
+    }
+    __syncthreads();
+    const double out = red[32];
+    __syncthreads();
+    return out;
+}
+
+// (h, l) += (h2, l2) in double-float arithmetic (Knuth's two-sum), FP32 only.
+__device__ __forceinline__ void ff_add(float &h, float &l, float h2, float l2)
+{
+    const float s = h + h2;
+    const float bb = s - h;
+    float e = (h - (s - bb)) + (h2 - bb);
+    e += l + l2;
+    h = s + e;
+    l = e - (h - s);
+}
+
+// Sum of (h + l) over the CTA, reduced in FP32 double-float; every thread
+// gets the double result.
+__device__ __forceinline__ double block_sum_ff(float h, float l, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, h, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, l, o);
+        ff_add(h, l, h2, l2);
+    }
+    float *rf = (float *)red;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) { rf[2 * wid] = h; rf[2 * wid + 1] = l; }
+    __syncthreads();
+    if (wid == 0) {
+        h = (lane < nw) ? rf[2 * lane] : 0.f;
+        l = (lane < nw) ? rf[2 * lane + 1] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, h, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, l, o);
+            ff_add(h, l, h2, l2);
+        }
+        if (lane == 0) red[32] = (double)h + (double)l;
+    }
+    __syncthreads();
+    const double out = red[32];
+    __syncthreads();
+    return out;
+}
+
+__device__ __forceinline__ double prior_term(const double *row, double x)
+{
+    const int id = (int)row[0];
+    if (id == 1) {
+        if (x < row[3] || x > row[4]) return -INFINITY;
+        if (!(row[2] > 0.0)) return -INFINITY;
+        const double z = (x - row[1]) / row[2];
+        return -0.5 * z * z + row[5];
+    }
+    if (x < row[1] || x > row[2]) return -INFINITY;
+    return row[5];
+}
+
+// Constant part of the truncated-normal log density:
+// -log(sqrt(2 pi)) - log(sigma) - log(Phi(b) - Phi(a)).
+__device__ __forceinline__ double tnorm_const(double mu, double sigma, double lo, double hi)
+{
+    if (!(sigma > 0.0)) return -INFINITY;
+    const double a = (lo - mu) / sigma, b = (hi - mu) / sigma;
+    double mass;
+    if (isinf(hi) && hi > 0) mass = 0.5 * erfc(a * 0.70710678118654752440);
+    else if (isinf(lo) && lo < 0) mass = 0.5 * erfc(-b * 0.70710678118654752440);
+    else mass = Phi64(b) - Phi64(a);
+    return -0.91893853320467274178 - log(sigma) - log(mass);
+}
+
+// Subject-level prior: fixed table, or the truncated normal of phi chain
+// `phi_chain` (src/de.cpp:599-603, 646-652).
+__device__ double sub_prior(const RunDev &r, const double *th, int phi_chain)
+{
+    double s = 0.0;
+    if (r.prior) {
+        for (int j = 0; j < r.P; ++j) s += prior_term(r.prior + kPriorRow * j, th[j]);
+    } else {
+        const double *pt = r.phi_tab + (size_t)phi_chain * r.P * 3;   // (mu, 1/sigma, c)
+        for (int j = 0; j < r.P; ++j) {
+            const double x = th[j];
+            double term;
+            if (x < r.pp_bounds[2 * j] || x > r.pp_bounds[2 * j + 1] || !(pt[3 * j + 1] > 0.0)) {
+                term = -INFINITY;
+            } else {
+                const double z = (x - pt[3 * j]) * pt[3 * j + 1];
+                term = -0.5 * z * z + pt[3 * j + 2];
+            }
+            s += term;
+        }
+    }
+    return s;
+}
+
+__device__ __forceinline__ double phi_prior(const RunDev &r, const double *th)
+{
+    double s = 0.0;
+    for (int j = 0; j < r.Pphi; ++j) s += prior_term(r.hprior + kPriorRow * j, th[j]);
+    return s;
+}
+
+// Metropolis test of update_theta (src/de.cpp:81-108): accept iff
+// u < exp(d), d = log posterior difference; NaN rejects.  FP64 instructions
+// are scarce on this GPU and this test sits on the serial decision path, so
+// FP32 decides unless u lies within the FP32 error bound of exp(d): expf is
+// within 2 ulp, rounding d to float moves exp(d) by at most |d| 2^-24
+// relative and the two products round once more.  Only inside that band is
+// the double exp evaluated, so the outcome equals u < exp(d) in FP64.
+__device__ __forceinline__ bool mh_accept(double d, double u)
+{
+    if (isnan(d)) return false;
+    if (d >= 0.0) return u < 1.0 || u < exp(d);
+    if (d < -746.0) return u < 0.0;             // exp(d) underflows to +0
+    if (d < -80.0) return u < exp(d);           // rare: exp(d) < 2e-35
+    const float df = (float)d;
+    const float e = expf(df);
+    const float m = 1e-6f + fabsf(df) * 1.2e-7f;
+    if (u < (double)(e * (1.f - m))) return true;
+    if (u > (double)(e * (1.f + m))) return false;
+    return u < exp(d);
+}
+
+// draw slots (include/ggdmc_gpu.h): base(step) = 2 + C + step*(Pn+3)
+__device__ __forceinline__ int64_t step_base(const RunDev &r, int step)
+{
+    return 2 + (int64_t)r.C + (int64_t)step * (r.Pn + 3);
+}
+
+__device__ __forceinline__ double jitter_draw(const RunDev &r, int64_t it, int lev, int pass, int step,
+                                              int j)
+{
+    const double lo = -r.rp, hi = r.rp;
+    const double u = uniform(r.ds, it, lev, pass, step_base(r, step) + 2 + j);
+    return __dadd_rn(lo, __dmul_rn(__dsub_rn(hi, lo), u));
+}
+
+__device__ __forceinline__ double accept_draw(const RunDev &r, int64_t it, int lev, int pass, int step)
+{
+    return uniform(r.ds, it, lev, pass, step_base(r, step) + 2 + r.Pn);
+}
+
+// get_chains (src/de.cpp:52-60): two distinct partners other than i
+__device__ __forceinline__ void partners(const RunDev &r, int64_t it, int lev, int pass, int i,
+                                         int &a, int &b)
+{
+    const int C = r.C;
+    const int64_t base = step_base(r, i);
+    const double u0 = uniform(r.ds, it, lev, pass, base);
+    const double u1 = uniform(r.ds, it, lev, pass, base + 1);
+    int r0 = (int)(u0 * (double)(C - 1));
+    if (r0 > C - 2) r0 = C - 2;
+    int r1 = (int)(u1 * (double)(C - 2));
+    if (r1 > C - 3) r1 = C - 3;
+    const int pa = (r0 < i) ? r0 : r0 + 1;
+    const int lo = pa < i ? pa : i, hi = pa < i ? i : pa;
+    int pb = r1;
+    if (pb >= lo) ++pb;
+    if (pb >= hi) ++pb;
+    a = pa;
+    b = pb;
+}
+
+// get_subchains (src/de.cpp:62-78) from uniforms u[1..C+1] drawn in
+// parallel; single thread.
+__device__ int subchains_from(int C, const double *u, int *sub, int *perm)
+{
+    int n = (int)ceil((double)C * u[1]);
+    if (n < 2) n = 2;
+    if (n > C) n = C;
+    for (int j = 0; j < C; ++j) perm[j] = j;
+    for (int j = 0; j < n; ++j) {
+        int q = j + (int)(u[2 + j] * (double)(C - j));
+        if (q > C - 1) q = C - 1;
+        const int t = perm[j]; perm[j] = perm[q]; perm[q] = t;
+    }
+    for (int j = 0; j < n; ++j) sub[j] = perm[j];
+    for (int j = 1; j < n; ++j) {
+        const int x = sub[j];
+        int q = j - 1;
+        while (q >= 0 && sub[q] > x) { sub[q + 1] = sub[q]; --q; }
+        sub[q + 1] = x;
+    }
+    return n;
+}
+
+// one component of a crossover proposal (src/de.cpp:111-142):
+// theta_i + (U(-rp,rp) + gamma (theta_a - theta_b))
+__device__ __forceinline__ double cross_comp(double gamma, double ti, double ta, double tb, double jit)
+{
+    return __dadd_rn(ti, __dadd_rn(jit, __dmul_rn(gamma, __dsub_rn(ta, tb))));
+}
+
+__device__ __forceinline__ bool updated(int j, int para, int nloop)
+{
+    return (para >= 0) ? (j == para) : (j < nloop);
+}
+
+// Re-proposals from the current state with the pass's stored jitter.
+__device__ __forceinline__ void cross_prop_j(double gamma, int para, int nloop, int P,
+                                             const double *ti, const double *ta, const double *tb,
+                                             const double *jit, double *out)
+{
+    for (int j = 0; j < P; ++j)
+        out[j] = updated(j, para, nloop) ? cross_comp(gamma, ti[j], ta[j], tb[j], jit[j]) : ti[j];
+}
+
+__device__ __forceinline__ void mig_prop_j(int para, int nloop, int P, const double *ts,
+                                           const double *jit, double *out)
+{
+    for (int j = 0; j < P; ++j) out[j] = updated(j, para, nloop) ? __dadd_rn(ts[j], jit[j]) : ts[j];
+}
+
+// --------------------------------------------------- subject likelihood
+struct SubSmem {
+    double *theta;   // kMaxTheta
+    double *e64;     // n_ent * 5
+    double *t064;    // n_t0
+    double *red;     // 33
+    float4 *e32a;    // n_ent
+    float2 *e32b;    // n_ent
+    float2 *t032;    // n_t0
+    uint8_t *cent;   // n_cell * n_acc
+    uint8_t *cw;     // n_cell
+    uint8_t *ct0;    // n_cell
+    int *flag;       // 4
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[11])
+{
+    size_t o = 0;
+    off[0] = o; o += sizeof(double) * kMaxTheta;
+    off[1] = o; o += sizeof(double) * 5 * m.n_ent;
+    off[2] = o; o += sizeof(double) * m.n_t0;
+    off[3] = o; o += sizeof(double) * 33;
+    o = align_up(o, 16);
+    off[4] = o; o += sizeof(float4) * m.n_ent;
+    off[5] = o; o += sizeof(float2) * m.n_ent;
+    off[6] = o; o += sizeof(float2) * m.n_t0;
+    off[7] = o; o += (size_t)m.n_cell * m.n_acc;
+    off[8] = o; o += m.n_cell;
+    off[9] = o; o += m.n_cell;
+    o = align_up(o, 16);
+    off[10] = o; o += sizeof(int) * 4;
+    return align_up(o, 16);
+}
+
+__host__ __device__ size_t sub_smem_bytes(const DevModel &m)
+{
+    size_t off[11];
+    return sub_smem_layout(m, off);
+}
+
+__device__ SubSmem carve(char *base, const DevModel &m)
+{
+    size_t off[11];
+    sub_smem_layout(m, off);
+    SubSmem s;
+    s.theta = (double *)(base + off[0]);
+    s.e64 = (double *)(base + off[1]);
+    s.t064 = (double *)(base + off[2]);
+    s.red = (double *)(base + off[3]);
+    s.e32a = (float4 *)(base + off[4]);
+    s.e32b = (float2 *)(base + off[5]);
+    s.t032 = (float2 *)(base + off[6]);
+    s.cent = (uint8_t *)(base + off[7]);
+    s.cw = (uint8_t *)(base + off[8]);
+    s.ct0 = (uint8_t *)(base + off[9]);
+    s.flag = (int *)(base + off[10]);
+    return s;
+}
+
+__device__ void load_design(const RunDev &r, SubSmem &sm)
+{
+    const int n = r.m.n_cell * r.m.n_acc;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sm.cent[i] = r.m.cell_ent[i];
+    for (int i = threadIdx.x; i < r.m.n_cell; i += blockDim.x) {
+        sm.cw[i] = r.m.cell_w[i];
+        sm.ct0[i] = r.m.cell_t0[i];
+    }
+}
+
+// FP64 tables of sm.theta: (A, b, v, s, Phi(v/s)) per tuple, t0 per source.
+__device__ void build_tables64(const RunDev &r, SubSmem &sm)
+{
+    for (int u = threadIdx.x; u < r.m.n_ent; u += blockDim.x) {
+        const EntSrc es = r.m.ent_src[u];
+        const double A = src_value(es.A, sm.theta, r.m.consts);
+        const double B = src_value(es.B, sm.theta, r.m.consts);
+        const double v = src_value(es.v, sm.theta, r.m.consts);
+        const double s = src_value(es.s, sm.theta, r.m.consts);
+        double *e = sm.e64 + 5 * u;
+        e[0] = A; e[1] = A + B; e[2] = v; e[3] = s; e[4] = Phi64(v / s);
+    }
+    for (int q = threadIdx.x; q < r.m.n_t0; q += blockDim.x)
+        sm.t064[q] = src_value(r.m.t0_src[q], sm.theta, r.m.consts);
+}
+
+// FP32 table entry u of theta.  The exponent-sensitive ratios b/s, (b-A)/s
+// and v/s are formed in FP64 and rounded once; the scale factors in FP32.
+// Returns false when the tuple is outside the FP32 form's domain.
+__device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, int u, float4 &a, float2 &bb)
+{
+    const EntSrc es = r.m.ent_src[u];
+    const double A = src_value(es.A, theta, r.m.consts);
+    const double B = src_value(es.B, theta, r.m.consts);
+    const double v = src_value(es.v, theta, r.m.consts);
+    const double s = src_value(es.s, theta, r.m.consts);
+    const double b = A + B;
+    const double is = 1.0 / s;
+    const float kap = (float)(v * is);
+    const float den = normcdff(kap), qv = normcdff(-kap);
+    const float iad = 1.f / ((float)A * den);
+    a = make_float4((float)(b * is), (float)((b - A) * is), kap, (float)s * iad);
+    bb = make_float2((float)v * iad, qv / den);
+    return A > 0.0 && s > 0.0 && den > 1e-30f && isfinite(a.x) && isfinite(a.y) && isfinite(a.z) &&
+           isfinite(a.w) && isfinite(bb.x) && isfinite(bb.y);
+}
+
+__device__ __forceinline__ float2 t0split(const RunDev &r, const double *theta, int q)
+{
+    const double t0 = src_value(r.m.t0_src[q], theta, r.m.consts);
+    const float hi = (float)t0;
+    return make_float2(hi, (float)(t0 - (double)hi));
+}
+
+// FP32 tables of sm.theta (sm.flag[0] = 1 when some tuple is outside the
+// FP32 form's domain).
+__device__ void build_tables32(const RunDev &r, SubSmem &sm)
+{
+    for (int u = threadIdx.x; u < r.m.n_ent; u += blockDim.x) {
+        float4 a;
+        float2 bb;
+        if (!entry32(r, sm.theta, u, a, bb)) sm.flag[0] = 1;
+        sm.e32a[u] = a;
+        sm.e32b[u] = bb;
+    }
+    for (int q = threadIdx.x; q < r.m.n_t0; q += blockDim.x) sm.t032[q] = t0split(r, sm.theta, q);
+}
+
+// Tables of proposal `item`, as k_sub_propose / repropose stored them.
+__device__ void load_tables32(const RunDev &r, size_t item, SubSmem &sm)
+{
+    for (int u = threadIdx.x; u < r.m.n_ent; u += blockDim.x) {
+        sm.e32a[u] = r.tab_a[item * r.m.n_ent + u];
+        sm.e32b[u] = r.tab_b[item * r.m.n_ent + u];
+    }
+    for (int q = threadIdx.x; q < r.m.n_t0; q += blockDim.x) sm.t032[q] = r.tab_t[item * r.m.n_t0 + q];
+    if (threadIdx.x == 0) sm.flag[0] = r.tab_bad[item];
+}
+
+// Store the FP32 tables of proposal `item` (one thread).
+__device__ void store_tables(const RunDev &r, size_t item, const double *theta)
+{
+    int bad = 0;
+    for (int u = 0; u < r.m.n_ent; ++u) {
+        float4 a;
+        float2 bb;
+        if (!entry32(r, theta, u, a, bb)) bad = 1;
+        r.tab_a[item * r.m.n_ent + u] = a;
+        r.tab_b[item * r.m.n_ent + u] = bb;
+    }
+    for (int q = 0; q < r.m.n_t0; ++q) r.tab_t[item * r.m.n_t0 + q] = t0split(r, theta, q);
+    r.tab_bad[item] = bad;
+}
+
+// Sum of per-trial log densities of subject level l at sm.theta on the whole
+// CTA (every thread gets the sum); sm.theta must be set and synchronised.
+// MIXED: FP32 first; the FP64 tables are built only when a trial of this CTA
+// needs the FP64 form, and only those trials use it.
+__device__ double sub_loglik_range(const RunDev &r, int l, int i0, int i1, SubSmem &sm, bool mixed,
+                                   bool tables_ready = false)
+{
+    const int64_t base = r.offs[l] + i0;
+    const int n = i1 - i0;
+    const int K = r.m.n_acc;
+    bool fp64_all = !mixed;
+    if (mixed) {
+        if (!tables_ready) {
+            if (threadIdx.x == 0) sm.flag[0] = 0;
+            __syncthreads();
+            build_tables32(r, sm);
+        }
+        __syncthreads();
+        fp64_all = sm.flag[0] != 0;
+    }
+    double acc64 = 0.0;
+    if (!fp64_all) {
+        float ks = 0.f, kc = 0.f;
+        int nfb = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int c = r.cell[base + i];
+            const float2 rt = r.rt32[base + i];
+            const float2 t0 = sm.t032[sm.ct0[c]];
+            const float t = (rt.x - t0.x) + (rt.y - t0.y);
+            float ld;
+            if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a, sm.e32b, ld)) {
+                const float y = ld - kc;        // Kahan-compensated FP32 sum
+                const float tt = ks + y;
+                kc = (tt - ks) - y;
+                ks = tt;
+            } else {
+                ++nfb;
+            }
+        }
+        if (!__syncthreads_or(nfb > 0)) return block_sum_ff(ks, -kc, sm.red);
+        acc64 = (double)ks - (double)kc;
+        {
+            build_tables64(r, sm);
+            __syncthreads();
+            if (nfb > 0) {
+                for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                    const int c = r.cell[base + i];
+                    const float2 rt = r.rt32[base + i];
+                    const float2 t0 = sm.t032[sm.ct0[c]];
+                    const float t = (rt.x - t0.x) + (rt.y - t0.y);
+                    float ld;
+                    if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a, sm.e32b, ld)) continue;
+                    int e8[kMaxAcc];
+                    for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
+                    acc64 += lba_logdens64(r.rt64[base + i] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c],
+                                           sm.e64);
+                }
+            }
+        }
+    } else {
+        build_tables64(r, sm);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int c = r.cell[base + i];
+            int e8[kMaxAcc];
+            for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
+            acc64 += lba_logdens64(r.rt64[base + i] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c], sm.e64);
+        }
+    }
+    return block_sum(acc64, sm.red);
+}
+
+__device__ __forceinline__ double sub_loglik_sum(const RunDev &r, int l, SubSmem &sm, bool mixed)
+{
+    return sub_loglik_range(r, l, 0, (int)(r.offs[l + 1] - r.offs[l]), sm, mixed);
+}
+
+// log-likelihood of proposal (l, k) on the whole CTA, written to ll_s
+__device__ void eval_item(const RunDev &r, int l, int k, SubSmem &sm, bool mixed)
+{
+    const size_t item = (size_t)l * r.C + k;
+    const double *th = r.th_s + item * r.P;
+    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
+    if (mixed) load_tables32(r, item, sm);
+    __syncthreads();
+    const double ll = sub_loglik_range(r, l, 0, (int)(r.offs[l + 1] - r.offs[l]), sm, mixed, mixed);
+    if (threadIdx.x == 0) {
+        r.ll_s[(size_t)l * r.C + k] = ll;
+        atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)(r.offs[l + 1] - r.offs[l]));
+    }
+}
+
+// --------------------------------------------------------- subject kernels
+// k_sub_propose: pass type, partners, stored draws and proposals of every
+// chain of every subject level, with their log priors.  grid = S.
+__global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int pass)
+{
+    __shared__ double s_u[kMaxChain + 2];
+    __shared__ int s_sub[kMaxChain];
+    __shared__ int s_perm[kMaxChain];
+    __shared__ int s_pa[kMaxChain], s_pb[kMaxChain];
+    __shared__ int s_type, s_n, s_para;
+    const int l = blockIdx.x;
+    const int lev = r.level0 + l;
+    const int64_t it = *r.iter;
+    const int C = r.C, P = r.P;
+    if (l == 0)
+        for (int q = threadIdx.x; q < r.n_round; q += blockDim.x) { r.qn[q] = 0; r.qc[q] = 0; }
+    if (threadIdx.x == 0) {
+        int type = PASS_CROSS, para = -1;
+        if (r.loop == LOOP_HCHAINS) {
+            const bool mig = uniform(r.ds, it, lev, pass, 0) < r.sub_mig;
+            type = mig ? PASS_MIG : PASS_CROSS;
+            para = r.sub_blocked ? pass : -1;
+        } else if (pass == 0) {
+            const bool mig = uniform(r.ds, it, lev, 0, 0) < r.sub_mig;
+            r.migrated[l] = mig;
+            type = mig ? PASS_MIG : PASS_CROSS;
+            para = (!mig && r.sub_blocked) ? 0 : -1;
+        } else {
+            type = r.migrated[l] ? PASS_SKIP : PASS_CROSS;
+            para = pass;
+        }
+        s_type = type;
+        s_para = para;
+    }
+    __syncthreads();
+    const int type = s_type, para = s_para;
+    if (type == PASS_MIG) {
+        for (int q = 1 + threadIdx.x; q < C + 2; q += blockDim.x)
+            s_u[q] = uniform(r.ds, it, lev, pass, q);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_n = subchains_from(C, s_u, s_sub, s_perm);
+            atomicAdd(&r.stats[ST_MIGRATIONS], 1ull);
+        }
+    } else if (threadIdx.x == 0) {
+        s_n = (type == PASS_SKIP) ? 0 : C;
+    }
+    __syncthreads();
+    const int n = s_n;
+    if (threadIdx.x == 0) {
+        r.ptype[l] = type;
+        r.nstep[l] = n;
+        r.rs_para[l] = para;
+        r.rs_decided[l] = 0;
+        r.rs_done[l] = (n == 0) ? 1 : 0;
+    }
+    for (int k = threadIdx.x; k < C; k += blockDim.x) {
+        r.rs_mod[(size_t)l * C + k] = 0;
+        r.rs_ver[(size_t)l * C + k] = 0;
+        r.rs_pend[(size_t)l * C + k] = 0;
+    }
+    if (n == 0) return;
+    const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
+    const double *th = r.th + (size_t)l * C * P;
+    double *ths = r.th_s + (size_t)l * C * P;
+    double *jit = r.jit + (size_t)l * C * P;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        if (type == PASS_CROSS) {
+            int a, b;
+            partners(r, it, lev, pass, k, a, b);
+            s_pa[k] = a;
+            s_pb[k] = b;
+            r.partner[((size_t)l * C + k) * 2] = a;
+            r.partner[((size_t)l * C + k) * 2 + 1] = b;
+        } else {
+            r.sub[(size_t)l * C + k] = s_sub[k];
+        }
+        r.accu[(size_t)l * C + k] = accept_draw(r, it, lev, pass, k);
+    }
+    __syncthreads();
+    // proposals, one thread per (step, parameter)
+    for (int q = threadIdx.x; q < n * P; q += blockDim.x) {
+        const int k = q / P, j = q % P;
+        const int src = (type == PASS_CROSS) ? k : s_sub[k];
+        const double ts = th[(size_t)src * P + j];
+        double out = ts;
+        if (updated(j, para, nloop)) {
+            const double jv = jitter_draw(r, it, lev, pass, k, j);
+            jit[(size_t)k * P + j] = jv;
+            out = (type == PASS_CROSS)
+                      ? cross_comp(r.gamma, ts, th[(size_t)s_pa[k] * P + j],
+                                   th[(size_t)s_pb[k] * P + j], jv)
+                      : __dadd_rn(ts, jv);
+        }
+        ths[(size_t)k * P + j] = out;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int owner = (type == PASS_CROSS) ? k : s_sub[k];
+        const double lp = sub_prior(r, ths + (size_t)k * P, owner);
+        r.lp_s[(size_t)l * C + k] = lp;
+        r.ll_s[(size_t)l * C + k] = 0.0;
+        r.need[(size_t)l * C + k] = (lp > -INFINITY) ? 1 : 0;
+        r.tab_bad[(size_t)l * C + k] = 0;
+    }
+    if (r.prec != PREC_MIXED) return;
+    __syncthreads();
+    const int NE = r.m.n_ent, NT = r.m.n_t0;
+    for (int q = threadIdx.x; q < n * (NE + NT); q += blockDim.x) {
+        const int k = q / (NE + NT), u = q % (NE + NT);
+        const size_t item = (size_t)l * C + k;
+        if (u < NE) {
+            float4 a;
+            float2 bb;
+            if (!entry32(r, ths + (size_t)k * P, u, a, bb)) r.tab_bad[item] = 1;
+            r.tab_a[item * NE + u] = a;
+            r.tab_b[item * NE + u] = bb;
+        } else {
+            r.tab_t[item * NT + (u - NE)] = t0split(r, ths + (size_t)k * P, u - NE);
+        }
+    }
+}
+
+// k_sub_loglik: the hot kernel.  One CTA per (level, step) item, items in
+// descending trial-count order (longest first keeps the tail short).
+__global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int32_t *items)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int32_t item = items[blockIdx.x];
+    const int l = item / r.C, k = item % r.C;
+    if (k >= r.nstep[l] || !r.need[(size_t)l * r.C + k]) return;
+    SubSmem sm = carve(smem_raw, r.m);
+    load_design(r, sm);
+    eval_item(r, l, k, sm, r.prec == PREC_MIXED);
+}
+
+// Working copy of one level's decision state in shared memory: the single
+// thread that takes the ordered decisions then touches no global memory.
+struct ScanSmem {
+    double *lp, *ll;       // [C] current state
+    double *lps, *lls;     // [n] proposals
+    double *accu;          // [n]
+    int *pa, *pb;          // [n] partners (crossover) / pa = subset (migration)
+    int16_t *ver;          // [n]
+    uint8_t *mod;          // [n]
+    uint8_t *flag;         // [n]
+    int *acc;              // [n] accepted steps of this scan
+    int *misc;             // [0] decided, [1] accepted count
+};
+
+__host__ __device__ inline size_t scan_smem_bytes(int C)
+{
+    return align_up((size_t)C * (5 * sizeof(double) + 3 * sizeof(int) + sizeof(int16_t) + 2) + 64, 16);
+}
+
+__device__ ScanSmem carve_scan(char *base, int C)
+{
+    ScanSmem s;
+    s.lp = (double *)base;
+    s.ll = s.lp + C;
+    s.lps = s.ll + C;
+    s.lls = s.lps + C;
+    s.accu = s.lls + C;
+    s.pa = (int *)(s.accu + C);
+    s.pb = s.pa + C;
+    s.acc = s.pb + C;
+    s.misc = s.acc + C;
+    s.ver = (int16_t *)(s.misc + 4);
+    s.mod = (uint8_t *)(s.ver + C);
+    s.flag = s.mod + C;
+    return s;
+}
+
+// Sum the chunk partials of re-evaluations queued by the previous round
+// (fixed order, so the result does not depend on scheduling).
+__device__ void finalize_pending(const RunDev &r, int l, int n)
+{
+    const int64_t N = r.offs[l + 1] - r.offs[l];
+    const int nch = (int)((N + r.chunk - 1) / r.chunk);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const size_t item = (size_t)l * r.C + k;
+        if (!r.rs_pend[item]) continue;
+        double s = 0.0;
+        for (int c = 0; c < nch; ++c) s += r.part[item * r.max_chunk + c];
+        r.ll_s[item] = s;
+        r.rs_pend[item] = 0;
+    }
+}
+
+// One ordered-decision pass over level l (all threads): load the state,
+// let thread 0 decide from the saved position while the speculative
+// proposals are valid, write the accepted rows back.  Returns the position.
+__device__ int decide(const RunDev &r, int l, int type, int n, ScanSmem &ss)
+{
+    const int C = r.C, P = r.P;
+    const size_t lc = (size_t)l * C;
+    for (int k = threadIdx.x; k < C; k += blockDim.x) {
+        ss.lp[k] = r.lp[lc + k];
+        ss.ll[k] = r.ll[lc + k];
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        ss.lps[k] = r.lp_s[lc + k];
+        ss.lls[k] = r.ll_s[lc + k];
+        ss.accu[k] = r.accu[lc + k];
+        ss.ver[k] = r.rs_ver[lc + k];
+        ss.mod[k] = r.rs_mod[lc + k];
+        if (type == PASS_CROSS) {
+            ss.pa[k] = r.partner[(lc + k) * 2];
+            ss.pb[k] = r.partner[(lc + k) * 2 + 1];
+        } else {
+            ss.pa[k] = r.sub[lc + k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int i = r.rs_decided[l], na = 0;
+        while (i < n) {
+            int dst;
+            if (type == PASS_CROSS) {
+                const int a = ss.pa[i], b = ss.pb[i], v = ss.ver[i];
+                if ((a >= v && a < i && ss.mod[a]) || (b >= v && b < i && ss.mod[b])) break;
+                dst = i;
+            } else {
+                if (i > 0 && ss.mod[i - 1] && ss.ver[i] < i) break;
+                dst = (i + 1 == n) ? ss.pa[0] : ss.pa[i + 1];
+            }
+            const double cur = (type == PASS_CROSS) ? ss.ll[dst] + ss.lp[dst] : ss.lp[dst] + ss.ll[dst];
+            bool ok = false;
+            if (mh_accept((ss.lps[i] + ss.lls[i]) - cur, ss.accu[i])) {
+                ss.lp[dst] = ss.lps[i];
+                ss.ll[dst] = ss.lls[i];
+                ss.acc[na++] = i;
+                ok = true;
+            }
+            ss.mod[i] = ok ? 1 : 0;
+            ++i;
+        }
+        ss.misc[0] = i;
+        ss.misc[1] = na;
+        r.rs_decided[l] = i;
+    }
+    __syncthreads();
+    const int d = ss.misc[0], na = ss.misc[1];
+    for (int q = threadIdx.x; q < na * P; q += blockDim.x) {
+        const int i = ss.acc[q / P], j = q % P;
+        const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? ss.pa[0] : ss.pa[i + 1]);
+        r.th[(lc + dst) * P + j] = r.th_s[(lc + i) * P + j];
+    }
+    for (int q = threadIdx.x; q < na; q += blockDim.x) {
+        const int i = ss.acc[q];
+        const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? ss.pa[0] : ss.pa[i + 1]);
+        r.lp[lc + dst] = ss.lp[dst];
+        r.ll[lc + dst] = ss.ll[dst];
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) r.rs_mod[lc + k] = ss.mod[k];
+    if (threadIdx.x == 0 && na) atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)na);
+    __syncthreads();
+    return d;
+}
+
+// Re-propose the steps of level l made stale by the decisions before
+// `decided`: for a crossover every later chain whose partner in
+// [ver, decided) moved (threads in parallel), for a migration step
+// `decided` (one thread).  flag[k] = 1 for each re-proposed step.
+__device__ void repropose(const RunDev &r, int l, int type, int n, int decided, uint8_t *flag)
+{
+    const int C = r.C, P = r.P;
+    const double *th = r.th + (size_t)l * C * P;
+    double *ths = r.th_s + (size_t)l * C * P;
+    const double *jit = r.jit + (size_t)l * C * P;
+    const int32_t *prt = r.partner + (size_t)l * C * 2;
+    const int32_t *sub = r.sub + (size_t)l * C;
+    const uint8_t *mod = r.rs_mod + (size_t)l * C;
+    int16_t *ver = r.rs_ver + (size_t)l * C;
+    const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
+    const int para = r.rs_para[l];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) flag[k] = 0;
+    __syncthreads();
+    if (type == PASS_CROSS) {
+        for (int k = decided + (int)threadIdx.x; k < n; k += blockDim.x) {
+            const int a = prt[2 * k], b = prt[2 * k + 1];
+            const int v = ver[k];
+            const bool stale = (a >= v && a < decided && mod[a]) || (b >= v && b < decided && mod[b]);
+            ver[k] = (int16_t)decided;
+            if (stale) {
+                cross_prop_j(r.gamma, para, nloop, P, th + (size_t)k * P, th + (size_t)a * P,
+                             th + (size_t)b * P, jit + (size_t)k * P, ths + (size_t)k * P);
+                const double lpv = sub_prior(r, ths + (size_t)k * P, k);
+                r.lp_s[(size_t)l * C + k] = lpv;
+                r.ll_s[(size_t)l * C + k] = 0.0;
+                r.need[(size_t)l * C + k] = (lpv > -INFINITY) ? 1 : 0;
+                if (r.prec == PREC_MIXED && lpv > -INFINITY)
+                    store_tables(r, (size_t)l * C + k, ths + (size_t)k * P);
+                flag[k] = 1;
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        const int k = decided;
+        mig_prop_j(para, nloop, P, th + (size_t)sub[k] * P, jit + (size_t)k * P, ths + (size_t)k * P);
+        const double lpv = sub_prior(r, ths + (size_t)k * P, sub[k]);
+        r.lp_s[(size_t)l * C + k] = lpv;
+        r.ll_s[(size_t)l * C + k] = 0.0;
+        r.need[(size_t)l * C + k] = (lpv > -INFINITY) ? 1 : 0;
+        if (r.prec == PREC_MIXED && lpv > -INFINITY)
+            store_tables(r, (size_t)l * C + k, ths + (size_t)k * P);
+        ver[k] = (int16_t)k;
+        flag[k] = 1;
+    }
+    __syncthreads();
+}
+
+// k_sub_round: one global round.  Per subject level (grid = S): sum the
+// previous round's partials, decide what can be decided, re-propose every
+// stale step and queue its trial chunks for k_sub_loglik_queue.
+__global__ void __launch_bounds__(kRoundThreads) k_sub_round(RunDev r, int pass, int round)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int l = blockIdx.x;
+    if (r.rs_done[l]) return;
+    ScanSmem ss = carve_scan(smem_raw, r.C);
+    const int type = r.ptype[l];
+    const int n = r.nstep[l];
+    finalize_pending(r, l, n);
+    __syncthreads();
+    const int decided = decide(r, l, type, n, ss);
+    if (threadIdx.x == 0) atomicAdd(&r.stats[ST_ROUNDS], 1ull);
+    if (decided >= n) {
+        if (threadIdx.x == 0) {
+            r.rs_done[l] = 1;
+            atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
+        }
+        return;
+    }
+    repropose(r, l, type, n, decided, ss.flag);
+    const int64_t N = r.offs[l + 1] - r.offs[l];
+    const int nch = (int)((N + r.chunk - 1) / r.chunk);
+    int32_t *q = r.queue + (size_t)round * r.S * r.C * r.max_chunk;
+    for (int k = decided + threadIdx.x; k < n; k += blockDim.x) {
+        if (!ss.flag[k]) continue;
+        atomicAdd(&r.stats[ST_REEVALS], 1ull);
+        const size_t item = (size_t)l * r.C + k;
+        if (!r.need[item] || nch == 0) continue;
+        for (int c = 0; c < nch; ++c) r.part[item * r.max_chunk + c] = 0.0;
+        r.rs_pend[item] = 1;
+        const int slot = atomicAdd(&r.qn[round], nch);
+        for (int c = 0; c < nch; ++c) q[slot + c] = (int32_t)(item * r.max_chunk + c);
+        atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)N);
+    }
+}
+
+// k_sub_loglik_queue: persistent CTAs take queued (proposal, trial chunk)
+// units (dynamic scheduling) and write each chunk's partial sum.
+__global__ void __launch_bounds__(kLikThreads) k_sub_loglik_queue(RunDev r, int round)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    __shared__ int s_unit;
+    const int nq = r.qn[round];
+    if (nq == 0) return;
+    SubSmem sm = carve(smem_raw, r.m);
+    load_design(r, sm);
+    const int32_t *q = r.queue + (size_t)round * r.S * r.C * r.max_chunk;
+    const bool mixed = r.prec == PREC_MIXED;
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(&r.qc[round], 1);
+        __syncthreads();
+        const int idx = s_unit;
+        if (idx >= nq) break;
+        const int unit = q[idx];
+        const int item = unit / r.max_chunk, c = unit % r.max_chunk;
+        const int l = item / r.C;
+        const double *th = r.th_s + (size_t)item * r.P;
+        for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
+        if (mixed) load_tables32(r, (size_t)item, sm);
+        __syncthreads();
+        const int N = (int)(r.offs[l + 1] - r.offs[l]);
+        const int i0 = c * r.chunk, i1 = min(N, i0 + r.chunk);
+        const double s = sub_loglik_range(r, l, i0, i1, sm, mixed, mixed);
+        if (threadIdx.x == 0) r.part[unit] = s;
+    }
+}
+
+// k_sub_resolve: finishes, within one CTA per subject, the decisions the
+// global rounds left (continuing from the saved position).
+__global__ void __launch_bounds__(kResolveThreads) k_sub_resolve(RunDev r, int pass, int level_begin)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int l = level_begin + blockIdx.x;
+    if (r.rs_done[l]) return;
+    const int type = r.ptype[l];
+    const int n = r.nstep[l];
+    const bool mixed = r.prec == PREC_MIXED;
+    SubSmem sm = carve(smem_raw, r.m);
+    ScanSmem ss = carve_scan(smem_raw + sub_smem_bytes(r.m), r.C);
+    load_design(r, sm);
+    finalize_pending(r, l, n);
+    __syncthreads();
+    int reevals = 0, rounds = 0;
+#ifdef GGDMC_PHASE_PROFILE
+    long long c_dec = 0, c_rep = 0, c_ev = 0, t_a;
+#define PH_T0() t_a = clock64()
+#define PH_ADD(x) x += clock64() - t_a
+#else
+#define PH_T0()
+#define PH_ADD(x)
+#endif
+    for (int round = 0; round <= n; ++round) {
+        ++rounds;
+        PH_T0();
+        const int decided = decide(r, l, type, n, ss);
+        PH_ADD(c_dec);
+        if (decided >= n) break;
+        PH_T0();
+        repropose(r, l, type, n, decided, ss.flag);
+        PH_ADD(c_rep);
+        PH_T0();
+        const int kend = (type == PASS_CROSS) ? n : decided + 1;
+        for (int k = decided; k < kend; ++k) {
+            if (!ss.flag[k]) continue;
+            ++reevals;
+            if (r.need[(size_t)l * r.C + k]) eval_item(r, l, k, sm, mixed);
+            __syncthreads();
+        }
+        PH_ADD(c_ev);
+    }
+#ifdef GGDMC_PHASE_PROFILE
+    if (threadIdx.x == 0 && *r.iter == 3)
+        printf("PHASE l=%d type=%d N=%d reevals=%d rounds=%d dec=%lld rep=%lld ev=%lld\n", l, type,
+               (int)(r.offs[l + 1] - r.offs[l]), reevals, rounds, c_dec, c_rep, c_ev);
+#endif
+    if (threadIdx.x == 0) {
+        r.rs_done[l] = 1;
+        atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
+        atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
+        atomicAdd(&r.stats[ST_ROUNDS], (unsigned long long)rounds);
+        atomicAdd(&r.stats[ST_FINISH], 1ull);
+    }
+}
+
+// ------------------------------------------------------------ phi level
+// Hyper log-likelihood (sumloghlike, src/de.cpp:245-270) of phi vector `phv`
+// (shared memory) against subject chain `chain`, or, for run_hyper, against
+// the fixed data rows.  Every thread gets the sum.  MIXED: terms in FP32,
+// sum in FP64.
+__device__ double hyper_sum(const RunDev &r, const double *phv, int chain, double *cst, double *red)
+{
+    // cst[p] = constant of the log density, cst[P + p] = 1 / sigma
+    const int P = r.Pphi / 2;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        cst[p] = tnorm_const(phv[p], phv[P + p], r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
+        cst[P + p] = 1.0 / phv[P + p];
+    }
+    __syncthreads();
+    const int nrow = r.hrows ? r.n_row : r.S;
+    const bool fp32 = r.prec == PREC_MIXED;
+    double acc = 0.0;
+    float accf = 0.f;
+    for (int idx = threadIdx.x; idx < nrow * P; idx += blockDim.x) {
+        const int s = idx / P, p = idx % P;
+        const double x = r.hrows ? r.hrows[(size_t)s * P + p]
+                                 : r.th[((size_t)s * r.C + chain) * r.P + p];
+        if (x < r.pp_bounds[2 * p] || x > r.pp_bounds[2 * p + 1] || !(phv[P + p] > 0.0)) {
+            acc = -INFINITY;
+        } else if (fp32) {
+            const float z = (float)(x - phv[p]) * (float)cst[P + p];
+            accf = fmaf(-0.5f * z, z, accf + (float)cst[p]);
+        } else {
+            const double z = (x - phv[p]) * cst[P + p];
+            acc += -0.5 * z * z + cst[p];
+        }
+    }
+    return block_sum(acc + (double)accf, red);
+}
+
+__global__ void __launch_bounds__(kPhiThreads) k_phi_propose(RunDev r, int pass)
+{
+    __shared__ double s_u[kMaxChain + 2];
+    __shared__ int s_sub[kMaxChain];
+    __shared__ int s_perm[kMaxChain];
+    __shared__ int s_pa[kMaxChain], s_pb[kMaxChain];
+    __shared__ int s_type, s_n, s_para;
+    const int64_t it = *r.iter;
+    const int C = r.C, P = r.Pphi;
+    if (threadIdx.x == 0) {
+        int type = PASS_CROSS, para = -1;
+        if (r.phi_loop == LOOP_HCHAINS) {
+            const bool mig = uniform(r.ds, it, 0, pass, 0) < r.pop_mig;
+            type = mig ? PASS_MIG : PASS_CROSS;
+            para = r.phi_blocked ? pass : -1;
+        } else if (pass == 0) {
+            const bool mig = uniform(r.ds, it, 0, 0, 0) < r.sub_mig;
+            r.pmigrated[0] = mig;
+            type = mig ? PASS_MIG : PASS_CROSS;
+            para = (!mig && r.phi_blocked) ? 0 : -1;
+        } else {
+            type = r.pmigrated[0] ? PASS_SKIP : PASS_CROSS;
+            para = pass;
+        }
+        s_type = type;
+        s_para = para;
+    }
+    __syncthreads();
+    const int type = s_type, para = s_para;
+    if (type == PASS_MIG) {
+        for (int q = 1 + threadIdx.x; q < C + 2; q += blockDim.x) s_u[q] = uniform(r.ds, it, 0, pass, q);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_n = subchains_from(C, s_u, s_sub, s_perm);
+            atomicAdd(&r.stats[ST_MIGRATIONS], 1ull);
+        }
+    } else if (threadIdx.x == 0) {
+        s_n = (type == PASS_SKIP) ? 0 : C;
+    }
+    __syncthreads();
+    const int n = s_n;
+    if (threadIdx.x == 0) {
+        r.pptype[0] = type;
+        r.pnstep[0] = n;
+    }
+    if (n == 0) return;
+    const int nloop = r.Pn;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        if (type == PASS_CROSS) {
+            int a, b;
+            partners(r, it, 0, pass, k, a, b);
+            s_pa[k] = a;
+            s_pb[k] = b;
+            r.ppartner[2 * k] = a;
+            r.ppartner[2 * k + 1] = b;
+        } else {
+            r.psub[k] = s_sub[k];
+        }
+        r.paccu[k] = accept_draw(r, it, 0, pass, k);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n * P; q += blockDim.x) {
+        const int k = q / P, j = q % P;
+        const int src = (type == PASS_CROSS) ? k : s_sub[k];
+        const double ts = r.pth[(size_t)src * P + j];
+        double out = ts;
+        if (updated(j, para, nloop)) {
+            const double jv = jitter_draw(r, it, 0, pass, k, j);
+            r.pjit[(size_t)k * P + j] = jv;
+            out = (type == PASS_CROSS)
+                      ? cross_comp(r.gamma, ts, r.pth[(size_t)s_pa[k] * P + j],
+                                   r.pth[(size_t)s_pb[k] * P + j], jv)
+                      : __dadd_rn(ts, jv);
+        }
+        r.pth_s[(size_t)k * P + j] = out;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double lp = phi_prior(r, r.pth_s + (size_t)k * P);
+        r.plp_s[k] = lp;
+        r.pll_s[k] = 0.0;
+        r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
+    }
+}
+
+// k_phi_eval: grid = 3*C; block (k, what): what 0 refresh of the step's
+// source chain, 1 the proposal, 2 refresh of a migration's destination.
+__global__ void __launch_bounds__(kPhiThreads) k_phi_eval(RunDev r)
+{
+    __shared__ double s_phi[kMaxTheta];
+    __shared__ double s_cst[2 * kMaxTheta];
+    __shared__ double s_red[33];
+    const int k = blockIdx.x / 3, what = blockIdx.x % 3;
+    const int type = r.pptype[0];
+    if (type == PASS_SKIP || k >= r.pnstep[0]) return;
+    const bool refresh = (r.phi_loop == LOOP_HCHAINS);
+    const int P = r.Pphi;
+    int chain;
+    const double *vec;
+    if (type == PASS_CROSS) {
+        if (what == 2) return;
+        if (what == 0 && !refresh) return;
+        chain = k;
+        vec = (what == 0) ? r.pth + (size_t)k * P : r.pth_s + (size_t)k * P;
+    } else {
+        const int src = r.psub[k];
+        const int dst = (k + 1 == r.pnstep[0]) ? r.psub[0] : r.psub[k + 1];
+        if (what != 1 && !refresh) return;
+        chain = (what == 2) ? dst : src;
+        vec = (what == 0) ? r.pth + (size_t)src * P
+              : (what == 1) ? r.pth_s + (size_t)k * P : r.pth + (size_t)dst * P;
+    }
+    if (what == 1 && !r.pneed[k]) return;
+    for (int j = threadIdx.x; j < P; j += blockDim.x) s_phi[j] = vec[j];
+    __syncthreads();
+    const double h = hyper_sum(r, s_phi, chain, s_cst, s_red);
+    if (threadIdx.x == 0) {
+        if (what == 0) r.pref_src[k] = h;
+        else if (what == 1) r.pll_s[k] = h;
+        else r.pref_next[k] = h;
+    }
+}
+
+__device__ double phi_reeval(const RunDev &r, const double *vec, int chain, double *s_phi,
+                             double *s_cst, double *s_red)
+{
+    for (int j = threadIdx.x; j < r.Pphi; j += blockDim.x) s_phi[j] = vec[j];
+    __syncthreads();
+    return hyper_sum(r, s_phi, chain, s_cst, s_red);
+}
+
+// k_phi_resolve: ordered decisions of the phi level (src/de.cpp:385-565).
+__global__ void __launch_bounds__(kPhiThreads) k_phi_resolve(RunDev r, int pass)
+{
+    __shared__ uint8_t s_mod[kMaxChain];
+    __shared__ int16_t s_ver[kMaxChain];
+    __shared__ uint8_t s_flag[kMaxChain];
+    __shared__ double s_phi[kMaxTheta];
+    __shared__ double s_cst[2 * kMaxTheta];
+    __shared__ double s_red[33];
+    __shared__ int s_decided, s_acc;
+    const int type = r.pptype[0];
+    if (type == PASS_SKIP) return;
+    const int C = r.C, P = r.Pphi;
+    const int n = r.pnstep[0];
+    const bool refresh = (r.phi_loop == LOOP_HCHAINS);
+    const int nloop = r.Pn;
+    int para;
+    if (r.phi_loop == LOOP_HCHAINS) para = r.phi_blocked ? pass : -1;
+    else para = (type == PASS_MIG) ? -1 : (r.phi_blocked ? pass : -1);
+    for (int k = threadIdx.x; k < C; k += blockDim.x) { s_mod[k] = 0; s_ver[k] = 0; s_flag[k] = 0; }
+    if (threadIdx.x == 0) { s_decided = 0; s_acc = 0; }
+    __syncthreads();
+    int reevals = 0;
+    for (int round = 0; round <= n; ++round) {
+        if (threadIdx.x == 0) {
+            int i = s_decided;
+            while (i < n) {
+                int dst;
+                if (type == PASS_CROSS) {
+                    const int a = r.ppartner[2 * i], b = r.ppartner[2 * i + 1];
+                    const int v = s_ver[i];
+                    if ((a >= v && a < i && s_mod[a]) || (b >= v && b < i && s_mod[b])) break;
+                    dst = i;
+                    if (refresh) r.pll[i] = r.pref_src[i];
+                } else {
+                    if (i > 0 && s_mod[i - 1] && s_ver[i] < i) break;
+                    const int src = r.psub[i];
+                    dst = (i + 1 == n) ? r.psub[0] : r.psub[i + 1];
+                    if (refresh) {
+                        r.pll[src] = r.pref_src[i];
+                        r.pll[dst] = r.pref_next[i];
+                    }
+                }
+                const double cur = (type == PASS_CROSS) ? r.pll[dst] + r.plp[dst]
+                                                        : r.plp[dst] + r.pll[dst];
+                bool ok = false;
+                if (mh_accept((r.plp_s[i] + r.pll_s[i]) - cur, r.paccu[i])) {
+                    for (int j = 0; j < P; ++j) r.pth[(size_t)dst * P + j] = r.pth_s[(size_t)i * P + j];
+                    r.plp[dst] = r.plp_s[i];
+                    r.pll[dst] = r.pll_s[i];
+                    ok = true;
+                    ++s_acc;
+                }
+                s_mod[i] = ok ? 1 : 0;
+                ++i;
+            }
+            s_decided = i;
+        }
+        __syncthreads();
+        const int decided = s_decided;
+        if (decided >= n) break;
+        if (type == PASS_CROSS) {
+            for (int k = decided + threadIdx.x; k < n; k += blockDim.x) {
+                const int a = r.ppartner[2 * k], b = r.ppartner[2 * k + 1];
+                const int v = s_ver[k];
+                const bool stale = (a >= v && a < decided && s_mod[a]) ||
+                                   (b >= v && b < decided && s_mod[b]);
+                s_ver[k] = (int16_t)decided;
+                s_flag[k] = stale ? 1 : 0;
+                if (stale) {
+                    cross_prop_j(r.gamma, para, nloop, P, r.pth + (size_t)k * P, r.pth + (size_t)a * P,
+                                 r.pth + (size_t)b * P, r.pjit + (size_t)k * P,
+                                 r.pth_s + (size_t)k * P);
+                    const double lp = phi_prior(r, r.pth_s + (size_t)k * P);
+                    r.plp_s[k] = lp;
+                    r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
+                    r.pll_s[k] = 0.0;
+                }
+            }
+        } else if (threadIdx.x == 0) {
+            const int k = decided;
+            mig_prop_j(para, nloop, P, r.pth + (size_t)r.psub[k] * P, r.pjit + (size_t)k * P,
+                       r.pth_s + (size_t)k * P);
+            const double lp = phi_prior(r, r.pth_s + (size_t)k * P);
+            r.plp_s[k] = lp;
+            r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
+            r.pll_s[k] = 0.0;
+            s_ver[k] = (int16_t)k;
+            s_flag[k] = 1;
+        }
+        __syncthreads();
+        const int kend = (type == PASS_CROSS) ? n : decided + 1;
+        for (int k = decided; k < kend; ++k) {
+            if (!s_flag[k]) continue;
+            const int chain = (type == PASS_CROSS) ? k : r.psub[k];
+            double h = 0.0;
+            if (r.pneed[k]) h = phi_reeval(r, r.pth_s + (size_t)k * P, chain, s_phi, s_cst, s_red);
+            if (type == PASS_MIG && refresh) {
+                const double hs = phi_reeval(r, r.pth + (size_t)chain * P, chain, s_phi, s_cst, s_red);
+                if (threadIdx.x == 0) r.pref_src[k] = hs;
+            }
+            if (threadIdx.x == 0) r.pll_s[k] = h;
+            __syncthreads();
+            ++reevals;
+        }
+        for (int k = decided + threadIdx.x; k < kend; k += blockDim.x) s_flag[k] = 0;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
+        atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)s_acc);
+        atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
+    }
+}
+
+// k_phi_tables: (mu, 1/sigma, c) of every phi chain for the subject priors.
+__global__ void k_phi_tables(RunDev r)
+{
+    const int i = blockIdx.x;
+    const int P = r.P;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        const double mu = r.pth[(size_t)i * r.Pphi + p];
+        const double sg = r.pth[(size_t)i * r.Pphi + P + p];
+        double *o = r.phi_tab + ((size_t)i * P + p) * 3;
+        o[0] = mu;
+        o[1] = (sg > 0.0) ? 1.0 / sg : 0.0;     // 0 marks an invalid scale
+        o[2] = tnorm_const(mu, sg, r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
+    }
+}
+
+// k_store: theta_class::store (thinned copy of the state into the samples).
+__global__ void k_store(RunDev r)
+{
+    const int64_t it = *r.iter;
+    if (it % r.thin != 0) return;
+    const int64_t slot = it / r.thin;
+    if (slot >= r.nmc) return;
+    const int l = blockIdx.x;
+    const size_t C = r.C;
+    if (l < r.S) {
+        const size_t P = r.P;
+        double *dt = r.smp_th + ((size_t)l * r.nmc + slot) * C * P;
+        const double *st = r.th + (size_t)l * C * P;
+        for (size_t j = threadIdx.x; j < C * P; j += blockDim.x) dt[j] = st[j];
+        for (size_t j = threadIdx.x; j < C; j += blockDim.x) {
+            r.smp_lp[((size_t)l * r.nmc + slot) * C + j] = r.lp[(size_t)l * C + j];
+            r.smp_ll[((size_t)l * r.nmc + slot) * C + j] = r.ll[(size_t)l * C + j];
+        }
+    } else if (r.Pphi > 0) {
+        const size_t P = r.Pphi;
+        for (size_t j = threadIdx.x; j < C * P; j += blockDim.x)
+            r.psmp_th[slot * C * P + j] = r.pth[j];
+        for (size_t j = threadIdx.x; j < C; j += blockDim.x) {
+            r.psmp_lp[slot * C + j] = r.plp[j];
+            r.psmp_ll[slot * C + j] = r.pll[j];
+        }
+    }
+}
+
+__global__ void k_next_iter(RunDev r)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *r.iter += 1;
+}
+
+// ------------------------------------------------- batch likelihood API
+// theta [S][n_theta][P] -> out [S][n_theta]; grid = S * n_theta.
+__global__ void __launch_bounds__(kLikThreads) k_loglik_batch(RunDev r, const double *theta,
+                                                              int n_theta, double *out)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int l = blockIdx.x / n_theta, k = blockIdx.x % n_theta;
+    SubSmem sm = carve(smem_raw, r.m);
+    const double *th = theta + ((size_t)l * n_theta + k) * r.P;
+    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
+    load_design(r, sm);
+    __syncthreads();
+    const double ll = sub_loglik_sum(r, l, sm, r.prec == PREC_MIXED);
+    if (threadIdx.x == 0) out[(size_t)l * n_theta + k] = ll;
+}
+
+// per-trial log densities of theta [S][P] -> out [N]; grid = S.
+__global__ void __launch_bounds__(kLikThreads) k_trial_logdens(RunDev r, const double *theta,
+                                                               double *out)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int l = blockIdx.x;
+    SubSmem sm = carve(smem_raw, r.m);
+    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = theta[(size_t)l * r.P + j];
+    load_design(r, sm);
+    if (threadIdx.x == 0) sm.flag[0] = 0;
+    __syncthreads();
+    const bool mixed = r.prec == PREC_MIXED;
+    if (mixed) build_tables32(r, sm);
+    build_tables64(r, sm);
+    __syncthreads();
+    const int64_t base = r.offs[l];
+    const int n = (int)(r.offs[l + 1] - base);
+    const int K = r.m.n_acc;
+    const bool use32 = mixed && sm.flag[0] == 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = r.cell[base + i];
+        if (use32) {
+            const float2 rt = r.rt32[base + i];
+            const float2 t0 = sm.t032[sm.ct0[c]];
+            const float t = (rt.x - t0.x) + (rt.y - t0.y);
+            float ld;
+            if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a, sm.e32b, ld)) {
+                out[base + i] = ld;
+                continue;
+            }
+        }
+        int e8[kMaxAcc];
+        for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
+        out[base + i] = lba_logdens64(r.rt64[base + i] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c], sm.e64);
+    }
+}
+
+// sumlogprior of n vectors against fixed rows; one thread per vector.
+__global__ void k_logprior(const double *rows, int P, const double *theta, int n, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int j = 0; j < P; ++j) s += prior_term(rows + kPriorRow * j, theta[(size_t)i * P + j]);
+    out[i] = s;
+}
+
+// sumloghlike of phi [n][2P] against subject thetas [S][n][P]; one CTA per phi.
+__global__ void __launch_bounds__(kPhiThreads) k_loghlike(RunDev r, const double *phi, double *out)
+{
+    __shared__ double s_phi[kMaxTheta];
+    __shared__ double s_cst[2 * kMaxTheta];
+    __shared__ double s_red[33];
+    const int j = blockIdx.x;
+    for (int q = threadIdx.x; q < r.Pphi; q += blockDim.x) s_phi[q] = phi[(size_t)j * r.Pphi + q];
+    __syncthreads();
+    const double h = hyper_sum(r, s_phi, j, s_cst, s_red);
+    if (threadIdx.x == 0) out[j] = h;
+}
+
+// ------------------------------------------------------------ launchers
+cudaError_t configure_kernels(const DevModel &m)
+{
+    const int bytes = (int)sub_smem_bytes(m);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_sub_loglik, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_sub_loglik_queue, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_sub_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  bytes + (int)scan_smem_bytes(kMaxChain))))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_sub_round, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)scan_smem_bytes(kMaxChain))))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_loglik_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    return cudaFuncSetAttribute(k_trial_logdens, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t launch_sub_propose(const RunDev &r, int pass, cudaStream_t st)
+{
+    k_sub_propose<<<r.S, kProposeThreads, 0, st>>>(r, pass);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, cudaStream_t st)
+{
+    k_sub_loglik<<<n_items, kLikThreads, sub_smem_bytes(r.m), st>>>(r, items);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_round(const RunDev &r, int pass, int round, cudaStream_t st)
+{
+    k_sub_round<<<r.S, kRoundThreads, scan_smem_bytes(r.C), st>>>(r, pass, round);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_loglik_queue(const RunDev &r, int round, int n_blocks, cudaStream_t st)
+{
+    k_sub_loglik_queue<<<n_blocks, kLikThreads, sub_smem_bytes(r.m), st>>>(r, round);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
+                               cudaStream_t st)
+{
+    k_sub_resolve<<<level_count, kResolveThreads, sub_smem_bytes(r.m) + scan_smem_bytes(r.C), st>>>(
+        r, pass, level_begin);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st)
+{
+    k_phi_tables<<<r.C, 32, 0, st>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phi_propose(const RunDev &r, int pass, cudaStream_t st)
+{
+    k_phi_propose<<<1, kPhiThreads, 0, st>>>(r, pass);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st)
+{
+    k_phi_eval<<<3 * r.C, kPhiThreads, 0, st>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phi_resolve(const RunDev &r, int pass, cudaStream_t st)
+{
+    k_phi_resolve<<<1, kPhiThreads, 0, st>>>(r, pass);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_store(const RunDev &r, cudaStream_t st)
+{
+    k_store<<<r.S + (r.Pphi > 0 ? 1 : 0), 256, 0, st>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_next_iter(const RunDev &r, cudaStream_t st)
+{
+    k_next_iter<<<1, 32, 0, st>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_theta, double *out,
+                                cudaStream_t st)
+{
+    k_loglik_batch<<<r.S * n_theta, kLikThreads, sub_smem_bytes(r.m), st>>>(r, theta, n_theta, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *out, cudaStream_t st)
+{
+    k_trial_logdens<<<r.S, kLikThreads, sub_smem_bytes(r.m), st>>>(r, theta, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
+                            cudaStream_t st)
+{
+    k_logprior<<<(n + 127) / 128, 128, 0, st>>>(rows, P, theta, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_loghlike(const RunDev &r, const double *phi, double *out, cudaStream_t st)
+{
+    k_loghlike<<<r.C, kPhiThreads, 0, st>>>(r, phi, out);
+    return cudaGetLastError();
+}
+
+}  // namespace ggdmc

@@ -1,0 +1,152 @@
+"""Seeded synthetic LBA workloads of the shapes the reference's benchmarks name.
+
+The race is simulated as the reference's fixture generators do with
+lbaModel::simulate (e.g. tests/testthat/Group1/data/6_lba_Bv_model.r:91-92):
+per trial and accumulator, start ~ U(0, A), drift ~ N(mean_v, sd_v) redrawn
+until positive, finish = (A + B - start) / drift; RT = t0 + min(finish) and
+the response is the argmin.  Subject parameters of hierarchical workloads
+are drawn from truncated normals (lower 0) around a population vector.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .design import (BV13_POP_MEAN, BV13_POP_SCALE, T0_17_P, design_bv13, design_rows,
+                     design_t0_17, vector)
+from .dmi import FlatModel, SubjectBatch, SubjectData
+
+PRIOR_ROW_UNIF_0_10 = [0.0, 10.0, 0.0, 10.0, 6.0, 1.0]
+
+
+def rtnorm(rng, mean, sd, lower=0.0, size=None):
+    """Truncated normal draws (lower bound) by rejection."""
+    mean = np.asarray(mean, float)
+    sd = np.asarray(sd, float)
+    out = rng.normal(mean, sd, size=size)
+    bad = out <= lower
+    while np.any(bad):
+        out = np.where(bad, rng.normal(mean, sd, size=out.shape), out)
+        bad = out <= lower
+    return out
+
+
+def simulate_subject(model: FlatModel, theta: np.ndarray, n: int, rng, name="") -> SubjectData:
+    """n trials spread evenly over the design's stimulus conditions."""
+    rows = design_rows(model)
+    cv = model.cell_values(theta)            # [n_cell, K, 6]
+    K = model.n_acc
+    counts = np.full(len(rows), n // len(rows))
+    counts[: n % len(rows)] += 1
+    rts, cells = [], []
+    for (prefix, cell_by_resp), m in zip(rows, counts):
+        if m == 0:
+            continue
+        p = cv[cell_by_resp[0]]              # accumulator parameters do not depend on the response
+        A, B, v, s, t0 = p[:, 0], p[:, 1], p[:, 2], p[:, 3], p[0, 4]
+        start = rng.random((m, K)) * A
+        drift = rng.normal(v, s, size=(m, K))
+        bad = drift <= 0
+        while np.any(bad):
+            drift = np.where(bad, rng.normal(v, s, size=(m, K)), drift)
+            bad = drift <= 0
+        finish = (A + B - start) / drift
+        w = np.argmin(finish, axis=1)
+        rts.append(t0 + finish[np.arange(m), w])
+        cells.append(np.array(cell_by_resp, np.int32)[w])
+    rt = np.concatenate(rts)
+    cell = np.concatenate(cells)
+    order = np.argsort(cell, kind="stable")  # DMI layout: trials grouped by cell
+    return SubjectData(rt[order], cell[order], name)
+
+
+@dataclass
+class Workload:
+    name: str
+    model: FlatModel
+    batch: SubjectBatch
+    theta_true: np.ndarray          # [S][P]
+    p_prior: np.ndarray             # [P][6]
+    h_prior: np.ndarray | None      # [2P][6]
+    pop_mean: np.ndarray | None
+    pop_scale: np.ndarray | None
+    nchain: int
+    hierarchical: bool
+
+
+def unif_prior(P, lo=0.0, hi=10.0):
+    return np.tile(np.array([lo, hi, lo, hi, 6.0, 1.0]), (P, 1))
+
+
+def tnorm_prior(mu, sigma, lo=0.0, hi=np.inf):
+    mu = np.asarray(mu, float)
+    return np.stack([mu, np.broadcast_to(sigma, mu.shape), np.full_like(mu, lo),
+                     np.full_like(mu, hi), np.full_like(mu, 1.0), np.ones_like(mu)], axis=1)
+
+
+def uneven_lba_256(seed: int = 1, n_subject: int = 256, n_lo: int = 100, n_hi: int = 2000,
+                   cv: float = 0.10) -> Workload:
+    """256 subjects, N_s ~ U{100..2000}, the 17-parameter 4-accumulator design,
+    subject theta ~ tnorm(pop, 10% CV, lower 0); hierarchical, 3 x npar chains."""
+    rng = np.random.default_rng(seed)
+    model = design_t0_17()
+    pop = vector(model, T0_17_P)
+    ns = rng.integers(n_lo, n_hi + 1, size=n_subject)
+    thetas, subs = [], []
+    for s in range(n_subject):
+        th = rtnorm(rng, pop, cv * pop)
+        thetas.append(th)
+        subs.append(simulate_subject(model, th, int(ns[s]), rng, str(s + 1)))
+    P = model.n_par
+    return Workload("uneven_lba_256", model, SubjectBatch.pack(subs), np.array(thetas),
+                    tnorm_prior(rng.random(P), 10.0),
+                    unif_prior(2 * P), pop, cv * pop, 3 * P, True)
+
+
+def hier_lba_32(seed: int = 0, n_subject: int = 32, n: int = 768) -> Workload:
+    """32 subjects x 768 trials of the 13-parameter design, theta from the
+    README's pop_mean / pop_scale truncated normals."""
+    rng = np.random.default_rng(seed)
+    model = design_bv13()
+    mu, sc = vector(model, BV13_POP_MEAN), vector(model, BV13_POP_SCALE)
+    thetas, subs = [], []
+    for s in range(n_subject):
+        th = rtnorm(rng, mu, sc)
+        thetas.append(th)
+        subs.append(simulate_subject(model, th, n, rng, str(s + 1)))
+    P = model.n_par
+    return Workload("hier_lba_32", model, SubjectBatch.pack(subs), np.array(thetas),
+                    tnorm_prior(rng.random(P), 10.0), unif_prior(2 * P), mu, sc, 3 * P, True)
+
+
+def many_fits_1024(seed: int = 4, n_fit: int = 1024, n_lo: int = 200, n_hi: int = 5000) -> Workload:
+    """1024 independent single-subject fits of the 13-parameter design; theta
+    from the 32-subject population, N ~ U{200..5000}; U(0,10) priors."""
+    rng = np.random.default_rng(seed)
+    model = design_bv13()
+    mu, sc = vector(model, BV13_POP_MEAN), vector(model, BV13_POP_SCALE)
+    ns = rng.integers(n_lo, n_hi + 1, size=n_fit)
+    thetas, subs = [], []
+    for s in range(n_fit):
+        th = rtnorm(rng, mu, sc)
+        thetas.append(th)
+        subs.append(simulate_subject(model, th, int(ns[s]), rng, str(s + 1)))
+    P = model.n_par
+    return Workload("many_fits_1024", model, SubjectBatch.pack(subs), np.array(thetas),
+                    unif_prior(P), None, None, None, 3 * P, False)
+
+
+def start_states(w: Workload, nchain: int, rng, spread: float = 0.05):
+    """Chains scattered around the generating values (theta [S][C][P] and,
+    for hierarchical workloads, phi [C][2P]); lp / ll left for the caller."""
+    S, P = w.theta_true.shape
+    th = w.theta_true[:, None, :] * (1.0 + spread * rng.standard_normal((S, nchain, P)))
+    th = np.abs(th)
+    phi = None
+    if w.hierarchical:
+        loc = w.pop_mean[None, :] * (1.0 + spread * rng.standard_normal((nchain, P)))
+        sca = w.pop_scale[None, :] * (1.0 + spread * rng.standard_normal((nchain, P)))
+        phi = np.concatenate([np.abs(loc), np.abs(sca)], axis=1)
+    return th, phi

@@ -52,6 +52,10 @@ enum { GGDMC_MODEL_LBA = 0, GGDMC_MODEL_DDM = 1 };
  *                 plain GPU form the batched kernels are measured against. */
 enum { GGDMC_FP64 = 0, GGDMC_MIXED = 1, GGDMC_FP64_PLAIN = 2 };
 
+/* ggdmc_de_config.flags: flush L2 between iterations and report in
+ * ggdmc_run_stats.sweep_ms only the iterations' own kernel time (benchmarks). */
+#define GGDMC_FLAG_L2_FLUSH 1
+
 /* Prior families, ggdmcPrior's dist_id codes (fixture lba_data*.rda). */
 enum { GGDMC_PRIOR_TNORM = 1, GGDMC_PRIOR_UNIF = 6 };
 
@@ -105,7 +109,7 @@ typedef struct {
     int32_t nmc;               /* stored samples, slot 0 = start state */
     int32_t thin;              /* iterations between stored samples    */
     int32_t precision;         /* GGDMC_FP64 / GGDMC_MIXED / GGDMC_FP64_PLAIN */
-    int32_t flags;             /* reserved, 0 */
+    int32_t flags;             /* GGDMC_FLAG_* bits, 0 by default */
     uint64_t seed;             /* key of the counter-based draw stream */
 } ggdmc_de_config;
 
@@ -131,6 +135,11 @@ typedef struct {
     int64_t migrations;        /* migration passes taken      */
     int64_t reevaluations;     /* speculative re-evaluations  */
     int64_t kernel_launches;   /* kernels launched by the run */
+    int64_t trial_evals;       /* per-trial densities evaluated */
+    int64_t iterations;        /* DE iterations (sweeps) run    */
+    double sweep_ms;           /* device time of the sweeps (CUDA events), ms */
+    int64_t resolve_rounds;    /* ordered-decision rounds over all subject passes */
+    int64_t resolve_finish;    /* subject passes finished by the in-CTA resolve */
 } ggdmc_run_stats;
 
 typedef struct ggdmc_handle ggdmc_handle;
@@ -255,6 +264,12 @@ ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg,
                               ggdmc_samples *phi_out,
                               ggdmc_samples *subj_out,
                               ggdmc_run_stats *stats);
+
+/* Measured throughput of this GPU's FP32 FMA pipe (TFLOP/s, 2 flops per
+ * FMA) and MUFU unit (tera-ops/s of ex2.approx): the roofline denominators of
+ * the likelihood kernel.  No counterpart in the reference (a measurement
+ * utility of this library). */
+ggdmc_status ggdmc_probe_peaks(double *fp32_tflops, double *mufu_tops);
 
 /* Message of this thread's last failed call ("" if none). */
 const char *ggdmc_last_error(void);

@@ -804,3 +804,9 @@ EXPORT double oracle_ddm_dens(double rt, const double *cv, int w)
 {
     return ddm_dens(rt, cv, w);
 }
+
+/* raw Philox4x32-10 block, for known-answer tests */
+EXPORT void oracle_philox(uint32_t *ctr, uint32_t k0, uint32_t k1)
+{
+    philox4x32_10(ctr, k0, k1);
+}

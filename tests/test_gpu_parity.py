@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA library (through its C ABI) against the CPU oracle.
+
+Tolerances:
+* FP64 path: per-subject log-likelihood sums within 1e-12 relative of the
+  oracle; chain states after a run bit-identical (same keyed draws, so the
+  same partners, subsets and accept decisions).
+* MIXED path: per-subject sums within 1e-6 relative to sum_i |log d_i| of the
+  FP64 oracle (the conditioning scale of a sum of per-trial log densities) at
+  parameters near the generating values.
+"""
+import numpy as np
+import pytest
+
+from conftest import PINNED_LBA_FIXTURES, load_fixture
+from ggdmc_gb300 import abi, gpu, synth
+from ggdmc_gb300.dmi import SubjectBatch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from ggdmc_gb300 import build
+    build.build()
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)) / np.maximum(np.abs(np.asarray(b)), 1e-300)
+
+
+@pytest.mark.parametrize("fx", PINNED_LBA_FIXTURES)
+def test_fp64_loglik_matches_oracle_and_golden(oracle, fx):
+    z, model, sub, pop = load_fixture(fx)
+    h = gpu.Handle(model, pop)
+    S = pop.n_subject
+    got = h.loglik(z["subj_theta"][:S], abi.FP64)
+    want = oracle.loglik(model, pop, z["subj_theta"][:S])
+    assert np.all(rel(got, want) <= 1e-12), rel(got, want).max()
+    assert np.all(rel(got, z["subj_ll"][:S]) <= 2e-9)
+    hs = gpu.Handle(model, sub)
+    got1 = hs.loglik(z["sub_theta"][None], abi.FP64)[0]
+    assert np.all(rel(got1, z["sub_ll"]) <= 2e-9)
+
+
+def test_fp64_per_trial_log_densities(oracle):
+    z, model, _, pop = load_fixture(6)
+    h = gpu.Handle(model, pop)
+    S = pop.n_subject
+    theta = z["subj_theta"][:S, 0]
+    got = h.trial_logdens(theta, abi.FP64)
+    for s in range(S):
+        a, b = pop.offsets[s], pop.offsets[s + 1]
+        _, want = oracle.sumloglike(model, pop.rt[a:b], pop.cell[a:b], theta[s], per_trial=True)
+        assert np.allclose(got[a:b], want, rtol=1e-12, atol=1e-12)
+
+
+def near_truth(w, n, rng, spread):
+    th = w.theta_true[:, None, :] * (1 + spread * rng.standard_normal((w.theta_true.shape[0], n,
+                                                                       w.theta_true.shape[1])))
+    return np.abs(th)
+
+
+@pytest.mark.parametrize("spread", [0.02, 0.05])
+def test_mixed_loglik_uneven_256(oracle, spread):
+    w = synth.uneven_lba_256(n_subject=64)
+    rng = np.random.default_rng(3)
+    theta = near_truth(w, 4, rng, spread)
+    h = gpu.Handle(w.model, w.batch)
+    mixed = h.loglik(theta, abi.MIXED)
+    fp64 = h.loglik(theta, abi.FP64)
+    want = oracle.loglik(w.model, w.batch, theta)
+    assert np.all(rel(fp64, want) <= 1e-12)
+    # conditioning scale: sum of |log d_i| per subject and theta
+    scale = np.zeros_like(want)
+    for s in range(w.batch.n_subject):
+        sd = w.batch.subject(s)
+        for j in range(theta.shape[1]):
+            _, per = oracle.sumloglike(w.model, sd.rt, sd.cell, theta[s, j], per_trial=True)
+            scale[s, j] = np.abs(per).sum()
+    err = np.abs(mixed - want) / scale
+    assert np.all(err <= 1e-6), err.max()
+
+
+def test_mixed_loglik_fixtures_close(oracle):
+    # prior draws of the fixtures: wild parameters, many FP64 re-evaluations
+    z, model, _, pop = load_fixture(6)
+    h = gpu.Handle(model, pop)
+    S = pop.n_subject
+    mixed = h.loglik(z["subj_theta"][:S], abi.MIXED)
+    want = oracle.loglik(model, pop, z["subj_theta"][:S])
+    assert np.all(rel(mixed, want) <= 1e-5), rel(mixed, want).max()
+
+
+def informative(z, C):
+    idx = np.argsort(z["sub_ll"])[::-1][:C]
+    return z["sub_theta"][idx].copy(), z["sub_lp"][idx].copy(), z["sub_ll"][idx].copy()
+
+
+@pytest.mark.parametrize("mig,blocked", [(0.0, False), (0.3, False), (0.15, True)])
+def test_run_subject_fp64_bit_exact(oracle, mig, blocked):
+    z, model, sub, _ = load_fixture(6)
+    th, lp, ll = informative(z, 39)
+    cfg = abi.DEConfigPy(nchain=39, nparameter=model.n_par, nmc=6, thin=2,
+                         sub_migration_prob=mig, is_pblocked=blocked, seed=2024)
+    g = gpu.run_subjects(cfg, model, sub, z["sub_prior"], th[None], lp[None], ll[None])
+    o = oracle.run_subjects(cfg, model, sub, z["sub_prior"], th[None], lp[None], ll[None])
+    assert np.array_equal(g["theta"], o["theta"])
+    assert np.array_equal(g["s_theta"], o["s_theta"])
+    assert np.allclose(g["ll"], o["ll"], rtol=1e-12)
+    assert np.allclose(g["s_lp"], o["s_lp"], rtol=1e-12)
+    assert g["stats"]["accepts"] == o["stats"].accepts > 0
+    assert g["stats"]["kernel_launches"] > 0
+
+
+def test_run_subject_host_fed_draws(oracle):
+    z, model, sub, _ = load_fixture(6)
+    th, lp, ll = informative(z, 15)
+    cfg = abi.DEConfigPy(nchain=15, nparameter=model.n_par, nmc=5, thin=1,
+                         sub_migration_prob=0.25, seed=0)
+    ni, npass, ns = abi.draw_layout(cfg, 1, False)
+    draws = np.random.default_rng(11).random(ni * npass * ns)
+    g = gpu.run_subjects(cfg, model, sub, z["sub_prior"], th[None], lp[None], ll[None], draws)
+    o = oracle.run_subjects(cfg, model, sub, z["sub_prior"], th[None], lp[None], ll[None], draws)
+    assert np.array_equal(g["theta"], o["theta"])
+
+
+@pytest.mark.parametrize("pm,sm,hb,pb", [(0.0, 0.0, False, False), (0.3, 0.3, False, False),
+                                         (0.2, 0.2, True, True)])
+def test_run_hierarchical_fp64_bit_exact(oracle, pm, sm, hb, pb):
+    z, model, _, pop = load_fixture(6)
+    S, C = 8, 26
+    batch = SubjectBatch(pop.rt[: pop.offsets[S]], pop.cell[: pop.offsets[S]],
+                         pop.offsets[: S + 1])
+    phi = (z["phi_theta"][:C], z["phi_lp"][:C], z["phi_ll"][:C])
+    subj = (z["subj_theta"][:S, :C], z["subj_lp"][:S, :C], z["subj_ll"][:S, :C])
+    cfg = abi.DEConfigPy(nchain=C, nparameter=2 * model.n_par, nmc=4, thin=1,
+                         pop_migration_prob=pm, sub_migration_prob=sm, is_hblocked=hb,
+                         is_pblocked=pb, seed=31)
+    g = gpu.run(cfg, model, batch, z["pop_p_prior"], z["pop_h_prior"], phi, subj)
+    o = oracle.run(cfg, model, batch, z["pop_p_prior"], z["pop_h_prior"], phi, subj)
+    assert np.array_equal(g["phi"][0], o["phi"][0])
+    assert np.allclose(g["phi"][2], o["phi"][2], rtol=1e-12)
+    assert np.array_equal(g["subj"][0], o["subj"][0])
+    assert np.allclose(g["subj"][2], o["subj"][2], rtol=1e-12)
+    assert np.array_equal(g["phi_s"][0], o["phi_s"][0])
+    assert g["stats"]["accepts"] == o["stats"].accepts
+
+
+def test_run_hyper_fp64_bit_exact(oracle):
+    z, model, _, _ = load_fixture(6)
+    rows = z["subj_theta"][:, 0, :]        # a subject-by-parameter matrix
+    C = 26
+    theta = z["phi_theta"][:C]
+    lp = oracle.logprior(z["pop_h_prior"], theta)
+    ll = oracle.loghlike(z["pop_p_prior"], theta, np.repeat(rows[:, None, :], C, axis=1))
+    cfg = abi.DEConfigPy(nchain=C, nparameter=2 * model.n_par, nmc=5, thin=1,
+                         sub_migration_prob=0.2, seed=8)
+    g = gpu.run_hyper(cfg, rows, z["pop_p_prior"], z["pop_h_prior"], theta, lp, ll)
+    o = oracle.run_hyper(cfg, rows, z["pop_p_prior"], z["pop_h_prior"], theta, lp, ll)
+    assert np.array_equal(g["theta"], o["theta"])
+    assert np.allclose(g["ll"], o["ll"], rtol=1e-12)
+
+
+def test_gpu_priors_match_oracle(oracle):
+    for fx in (3, 6):
+        z, *_ = load_fixture(fx)
+        assert np.allclose(gpu.logprior(z["sub_prior"], z["sub_theta"]), z["sub_lp"], rtol=1e-12)
+        got = gpu.loghlike(z["pop_p_prior"], z["phi_theta"], z["subj_theta"])
+        assert np.allclose(got, z["phi_ll"], rtol=1e-12)
+
+
+def test_many_fits_match_oracle(oracle):
+    w = synth.many_fits_1024(n_fit=6, n_lo=50, n_hi=300)
+    rng = np.random.default_rng(0)
+    C = 39
+    th, _ = synth.start_states(w, C, rng)
+    lp = np.stack([oracle.logprior(w.p_prior, th[f]) for f in range(6)])
+    ll = oracle.loglik(w.model, w.batch, th)
+    cfg = abi.DEConfigPy(nchain=C, nparameter=w.model.n_par, nmc=4, thin=1,
+                         sub_migration_prob=0.06, seed=4)
+    g = gpu.run_subjects(cfg, w.model, w.batch, w.p_prior, th, lp, ll)
+    o = oracle.run_subjects(cfg, w.model, w.batch, w.p_prior, th, lp, ll)
+    assert np.array_equal(g["theta"], o["theta"])
+
+
+def test_edge_empty_subject_and_floor(oracle):
+    z, model, sub, _ = load_fixture(6)
+    rt = np.concatenate([sub.rt[:10], sub.rt[:0], sub.rt[:5]])
+    cell = np.concatenate([sub.cell[:10], sub.cell[:0], sub.cell[:5]])
+    batch = SubjectBatch(rt, cell, np.array([0, 10, 10, 15], np.int64))
+    h = gpu.Handle(model, batch)
+    th = np.repeat(z["sub_theta"][None, :2], 3, axis=0)
+    th[:, 1, model.pnames.index("t0")] = 50.0        # t0 beyond every RT: all floors
+    got = h.loglik(th, abi.FP64)
+    assert got[1, 0] == 0.0 and got[1, 1] == 0.0     # no trials, no log-likelihood
+    assert np.allclose(got[0, 1], 10 * np.log(1e-10), rtol=1e-13)
+    want = oracle.loglik(model, batch, th)
+    assert np.allclose(got, want, rtol=1e-12)
+
+
+def test_invalid_inputs_are_errors():
+    z, model, sub, _ = load_fixture(6)
+    bad = SubjectBatch(sub.rt[:5], np.full(5, model.n_cell + 3, np.int32), np.array([0, 5]))
+    with pytest.raises(gpu.GGDMCError) as e:
+        gpu.Handle(model, bad)
+    assert e.value.status == abi.GGDMC_ERR_ARG
+    cfg = abi.DEConfigPy(nchain=2, nparameter=model.n_par, nmc=2)
+    th, lp, ll = informative(z, 2)
+    with pytest.raises(gpu.GGDMCError):
+        gpu.run_subjects(cfg, model, sub, z["sub_prior"], th[None], lp[None], ll[None])
+    prior = z["sub_prior"].copy()
+    prior[0, 4] = 3.0                                # unsupported dist_id
+    cfg = abi.DEConfigPy(nchain=3, nparameter=model.n_par, nmc=2)
+    th, lp, ll = informative(z, 3)
+    with pytest.raises(gpu.GGDMCError):
+        gpu.run_subjects(cfg, model, sub, prior, th[None], lp[None], ll[None])
