@@ -131,14 +131,11 @@ struct ggdmc_handle {
     DevBuf<double> th, lp, ll, th_s, lp_s, ll_s, phi_tab, pp_bounds, prior, hprior, hrows;
     DevBuf<double> pth, plp, pll, pth_s, plp_s, pll_s, pref_src, pref_next;
     DevBuf<int32_t> partner, ptype, nstep, sub, migrated, ppartner, pptype, pnstep, psub,
-        pmigrated, iter, status, items, items_plain, rs_decided, rs_para, queue, qn, qc;
+        pmigrated, iter, status, items, items_plain, rs_para;
     DevBuf<int8_t> need, pneed;
-    DevBuf<uint8_t> rs_done, rs_mod, rs_pend;
-    DevBuf<double> part;
     DevBuf<float4> tab_a;
     DevBuf<float2> tab_b, tab_t;
     DevBuf<int32_t> tab_bad;
-    DevBuf<int16_t> rs_ver;
     DevBuf<double> jit, accu, pjit, paccu;
     DevBuf<double> smp_th, smp_lp, smp_ll, psmp_th, psmp_lp, psmp_ll, draws;
     DevBuf<unsigned long long> stats;
@@ -399,30 +396,30 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     const int64_t n_slot = GGDMC_DRAW_SLOTS(C, c.nparameter);
 
     // ---- device buffers
+    const int CS = 2 * C;   // speculative proposals, then migration variants
+    int spec_group = 4;
+    if (const char *gs = std::getenv("GGDMC_SPEC_GROUP")) spec_group = std::min(4, std::max(1, std::atoi(gs)));
+    int n_spec_items = 0;
     if (S > 0) {
         CU(h->th.alloc((size_t)S * C * P));
         CU(h->lp.alloc((size_t)S * C));
         CU(h->ll.alloc((size_t)S * C));
-        CU(h->th_s.alloc((size_t)S * C * P));
-        CU(h->lp_s.alloc((size_t)S * C));
-        CU(h->ll_s.alloc((size_t)S * C));
+        CU(h->th_s.alloc((size_t)S * CS * P));
+        CU(h->lp_s.alloc((size_t)S * CS));
+        CU(h->ll_s.alloc((size_t)S * CS));
         CU(h->partner.alloc((size_t)S * C * 2));
-        CU(h->need.alloc((size_t)S * C));
+        CU(h->need.alloc((size_t)S * CS));
         CU(h->ptype.alloc(S));
         CU(h->nstep.alloc(S));
         CU(h->sub.alloc((size_t)S * C));
         CU(h->migrated.alloc(S));
         CU(h->jit.alloc((size_t)S * C * P));
         CU(h->accu.alloc((size_t)S * C));
-        CU(h->rs_decided.alloc(S));
         CU(h->rs_para.alloc(S));
-        CU(h->rs_done.alloc(S));
-        CU(h->rs_mod.alloc((size_t)S * C));
-        CU(h->rs_ver.alloc((size_t)S * C));
-        CU(h->tab_a.alloc((size_t)S * C * h->n_ent));
-        CU(h->tab_b.alloc((size_t)S * C * h->n_ent));
-        CU(h->tab_t.alloc((size_t)S * C * h->n_t0));
-        CU(h->tab_bad.alloc((size_t)S * C));
+        CU(h->tab_a.alloc((size_t)S * CS * h->n_ent));
+        CU(h->tab_b.alloc((size_t)S * CS * h->n_ent));
+        CU(h->tab_t.alloc((size_t)S * CS * h->n_t0));
+        CU(h->tab_bad.alloc((size_t)S * CS));
         CU(h->smp_th.alloc((size_t)S * nmc * C * P));
         CU(h->smp_lp.alloc((size_t)S * nmc * C));
         CU(h->smp_ll.alloc((size_t)S * nmc * C));
@@ -444,9 +441,12 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
             return (h->h_offs[x + 1] - h->h_offs[x]) > (h->h_offs[y + 1] - h->h_offs[y]);
         });
-        std::vector<int32_t> items((size_t)S * C), plain((size_t)S * C);
-        for (int q = 0; q < S; ++q)
-            for (int k = 0; k < C; ++k) items[(size_t)q * C + k] = order[q] * C + k;
+        std::vector<int32_t> items, plain((size_t)S * CS);
+        for (int q = 0; q < S; ++q) {
+            for (int k = 0; k < C; k += spec_group) items.push_back(order[q] * CS + k);
+            for (int k = C; k < CS; k += spec_group) items.push_back(order[q] * CS + k);
+        }
+        n_spec_items = (int)items.size();
         for (size_t q = 0; q < plain.size(); ++q) plain[q] = (int32_t)q;
         CU(h->items.upload(items.data(), items.size(), st));
         CU(h->items_plain.upload(plain.data(), plain.size(), st));
@@ -488,19 +488,6 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     const int64_t n_draw = n_iter * n_level * n_pass_draw * n_slot;
     if (a.draws) CU(h->draws.upload(a.draws, (size_t)n_draw, st));
     const bool plain = c.precision == GGDMC_FP64_PLAIN;
-    int n_round = 0;
-    if (const char *rs = std::getenv("GGDMC_ROUNDS")) n_round = std::max(0, std::atoi(rs));
-    if (plain || S == 0) n_round = 0;
-    int chunk = 256;
-    if (const char *cs = std::getenv("GGDMC_CHUNK")) chunk = std::max(32, std::atoi(cs));
-    int64_t max_n = 0;
-    for (int l = 0; l < S; ++l) max_n = std::max<int64_t>(max_n, h->h_offs[l + 1] - h->h_offs[l]);
-    const int max_chunk = (int)std::max<int64_t>(1, (max_n + chunk - 1) / chunk);
-    CU(h->qn.alloc(std::max(n_round, 1)));
-    CU(h->qc.alloc(std::max(n_round, 1)));
-    CU(h->queue.alloc((size_t)std::max(n_round, 1) * std::max(S, 1) * C * max_chunk));
-    CU(h->part.alloc((size_t)std::max(S, 1) * C * max_chunk));
-    CU(h->rs_pend.alloc((size_t)std::max(S, 1) * C));
     CU(h->iter.alloc(1));
     CU(h->status.alloc(1));
     CU(h->stats.alloc(ST_N));
@@ -533,10 +520,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.sub = h->sub.p; r.migrated = h->migrated.p;
     r.jit = h->jit.p; r.accu = h->accu.p;
     r.tab_a = h->tab_a.p; r.tab_b = h->tab_b.p; r.tab_t = h->tab_t.p; r.tab_bad = h->tab_bad.p;
-    r.rs_decided = h->rs_decided.p; r.rs_para = h->rs_para.p; r.rs_done = h->rs_done.p;
-    r.rs_mod = h->rs_mod.p; r.rs_ver = h->rs_ver.p;
-    r.queue = h->queue.p; r.qn = h->qn.p; r.qc = h->qc.p; r.n_round = n_round;
-    r.part = h->part.p; r.rs_pend = h->rs_pend.p; r.chunk = chunk; r.max_chunk = max_chunk;
+    r.rs_para = h->rs_para.p; r.CS = CS;
     r.pjit = h->pjit.p; r.paccu = h->paccu.p;
     r.prior = (!hier && !hyper) ? h->prior.p : nullptr;
     r.pp_bounds = (hier || hyper) ? h->pp_bounds.p : nullptr;
@@ -555,7 +539,6 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.status = h->status.p;
 
     int64_t launches_per_iter = 0;
-    const int queue_blocks = h->n_sm * 8;
     // One DE iteration (src/de.cpp:201-242 / 272-383) as a launch sequence.
     auto one_iteration = [&]() -> cudaError_t {
         cudaError_t e;
@@ -581,18 +564,14 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
                 ++launches_per_iter;
                 if (plain) {
                     for (int l = 0; l < S; ++l) {
-                        if ((e = launch_sub_loglik(r, h->items_plain.p + (size_t)l * C, C, st))) return e;
+                        if ((e = launch_sub_loglik(r, h->items_plain.p + (size_t)l * CS, CS, 1, st))) return e;
                         if ((e = launch_sub_resolve(r, p, l, 1, st))) return e;
                         launches_per_iter += 2;
                     }
                 } else {
-                    if ((e = launch_sub_loglik(r, h->items.p, S * C, st))) return e;
-                    for (int rd = 0; rd < n_round; ++rd) {
-                        if ((e = launch_sub_round(r, p, rd, st))) return e;
-                        if ((e = launch_sub_loglik_queue(r, rd, queue_blocks, st))) return e;
-                    }
+                    if ((e = launch_sub_loglik(r, h->items.p, n_spec_items, spec_group, st))) return e;
                     if ((e = launch_sub_resolve(r, p, 0, S, st))) return e;
-                    launches_per_iter += 2 + 2 * n_round;
+                    launches_per_iter += 2;
                 }
             }
         }
@@ -752,7 +731,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         a.stats->kernel_launches = launches;
         a.stats->trial_evals = (int64_t)hs[ST_TRIALS];
         a.stats->resolve_rounds = (int64_t)hs[ST_ROUNDS];
-        a.stats->resolve_finish = (int64_t)hs[ST_FINISH];
+        a.stats->variants = (int64_t)hs[ST_VARIANTS];
         a.stats->iterations = n_iter;
         a.stats->sweep_ms = sweep_ms;
     }

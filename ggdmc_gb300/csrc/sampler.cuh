@@ -24,7 +24,13 @@ enum LoopKind : int32_t {
 constexpr int kPriorRow = 6;
 
 enum StatIdx { ST_PROPOSALS = 0, ST_ACCEPTS, ST_MIGRATIONS, ST_REEVALS, ST_TRIALS, ST_ROUNDS,
-               ST_FINISH, ST_N };
+               ST_VARIANTS, ST_N };
+
+// Migration steps evaluated ahead per in-CTA round under the assumption that
+// the steps before them accept (a migration cascade carries one value
+// forward); the first round's cascade is evaluated with the speculative
+// proposals.
+constexpr int kVariants = 8;
 
 struct RunDev {
     // ------------------------------------------------------------ shape
@@ -54,33 +60,22 @@ struct RunDev {
 
     // ----------------------------------------------------- subject levels
     double *th, *lp, *ll;          // [S][C][P], [S][C]
-    double *th_s, *lp_s, *ll_s;    // proposals by step
+    double *th_s, *lp_s, *ll_s;    // [S][CS][P], [S][CS]: proposals by step, then variants
     int32_t *partner;              // [S][C][2]
-    int8_t *need;                  // [S][C]
+    int8_t *need;                  // [S][CS]
     int32_t *ptype;                // [S]
     int32_t *nstep;                // [S]
     int32_t *sub;                  // [S][C]
     int32_t *migrated;             // [S] (LOOP_CHAINS: migration taken this iteration)
     double *jit;                   // [S][C][P] jitter draws of the pass (re-proposals reuse them)
     double *accu;                  // [S][C]    Metropolis accept uniforms of the pass
-    // ordered-decision state of a pass, kept across the global rounds
-    int32_t *rs_decided;           // [S] next step to decide
     int32_t *rs_para;              // [S] blocked parameter of the pass, -1 for all
-    uint8_t *rs_done;              // [S]
-    uint8_t *rs_mod;               // [S][C] crossover: chain moved; migration: step accepted
-    int16_t *rs_ver;               // [S][C] decided prefix a proposal was built against
-    int32_t *queue;                // [n_round][S*C] (level*C + step) items to evaluate
-    int32_t *qn, *qc;              // [n_round] work units pushed / claimed
-    int32_t n_round;
-    double *part;                  // [S*C][max_chunk] partial sums of queued re-evaluations
-    // FP32 tables of every proposal, built where the proposal is built
-    float4 *tab_a;                 // [S*C][n_ent] (b/s, (b-A)/s, v/s, s/(A Phi(v/s)))
-    float2 *tab_b;                 // [S*C][n_ent] (v/(A Phi(v/s)), Phi(-v/s)/Phi(v/s))
-    float2 *tab_t;                 // [S*C][n_t0]  t0 as (hi, lo)
-    int32_t *tab_bad;              // [S*C] 1: outside the FP32 form's domain
-    uint8_t *rs_pend;              // [S][C] re-evaluation whose partials await summation
-    int32_t chunk;                 // trials per work unit of the queue
-    int32_t max_chunk;             // chunks of the longest subject
+    int32_t CS;                    // proposal slots per level: C speculative + C variants
+    // FP32 tables of every proposal slot, built where the proposal is built
+    float4 *tab_a;                 // [S*CS][n_ent] (b/s, (b-A)/s, v/s, s/(A Phi(v/s)))
+    float2 *tab_b;                 // [S*CS][n_ent] (v/(A Phi(v/s)), Phi(-v/s)/Phi(v/s))
+    float2 *tab_t;                 // [S*CS][n_t0]  t0 as (hi, lo)
+    int32_t *tab_bad;              // [S*CS] 1: outside the FP32 form's domain
     const double *prior;           // [P][kPriorRow] fixed subject prior (nullptr in HB)
     const double *pp_bounds;       // [P][2] p_prior (lower, upper) for HB / phi level
     double *phi_tab;               // [C][P][3] (mu, 1/sigma, c) of phi chain (HB)
@@ -108,11 +103,10 @@ struct RunDev {
 // --------------------------------------------------------------- launchers
 // (defined in sampler_kernels.cu)
 cudaError_t launch_sub_propose(const RunDev &r, int pass, cudaStream_t st);
-cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, cudaStream_t st);
+cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, int group,
+                              cudaStream_t st);
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
                                cudaStream_t st);
-cudaError_t launch_sub_round(const RunDev &r, int pass, int round, cudaStream_t st);
-cudaError_t launch_sub_loglik_queue(const RunDev &r, int round, int n_blocks, cudaStream_t st);
 cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st);
 cudaError_t launch_phi_propose(const RunDev &r, int pass, cudaStream_t st);
 cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st);

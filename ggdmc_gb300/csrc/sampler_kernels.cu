@@ -4,24 +4,20 @@
 // sequence, captured into a CUDA graph by the host runtime:
 //
 //   phi level:  k_phi_propose -> k_phi_eval -> k_phi_resolve -> k_phi_tables
-//   subjects:   k_sub_propose -> k_sub_loglik
-//               -> [k_sub_round -> k_sub_loglik_queue] x n_round
-//               -> k_sub_resolve                              (per pass)
+//   subjects:   k_sub_propose -> k_sub_loglik -> k_sub_resolve   (per pass)
 //   k_store -> k_next_iter
 //
 // The reference updates chains in place and in order (src/de.cpp:111-155):
 // chain i's partners may already have moved earlier in the same sweep.  The
 // kernels keep exactly that semantics by speculation.  k_sub_propose builds
 // every chain's proposal from the start-of-pass state and k_sub_loglik
-// evaluates all of them at once (the hot path: one CTA per (subject, chain),
-// trials striped over its threads).  Each k_sub_round then walks every
-// subject's chains in order, taking Metropolis decisions from the
-// speculative results for as long as a proposal is still the one the
-// sequential algorithm would have built; every chain made stale by an
-// accepted partner is re-proposed from the current state and queued, and
-// k_sub_loglik_queue evaluates the queue across the whole GPU.  k_sub_resolve
-// finishes, within one CTA per subject, what the rounds left.  Given the
-// same draws, the accepted states equal the sequential sampler's.
+// evaluates all of them at once (the hot path: each CTA evaluates up to four
+// proposals of one subject, trials striped over its threads).  k_sub_resolve
+// then walks each subject's steps in order on one CTA, taking Metropolis
+// decisions from the speculative results for as long as a proposal is the
+// one the sequential algorithm would have built, and re-proposes and
+// re-evaluates the rest round by round.  Given the same draws the accepted
+// states equal the sequential sampler's.
 #include <cfloat>
 #include <cstdio>
 #include <cstdint>
@@ -31,8 +27,7 @@
 namespace ggdmc {
 
 constexpr int kLikThreads = 128;
-constexpr int kResolveThreads = 256;
-constexpr int kRoundThreads = 64;
+constexpr int kResolveThreads = 384;
 constexpr int kPhiThreads = 256;
 constexpr int kProposeThreads = 128;
 
@@ -265,18 +260,20 @@ __device__ __forceinline__ void mig_prop_j(int para, int nloop, int P, const dou
 }
 
 // --------------------------------------------------- subject likelihood
+constexpr int kGroup = 4;   // proposals evaluated together per pass over the trials
+
 struct SubSmem {
-    double *theta;   // kMaxTheta
+    double *theta;   // [kGroup][kMaxTheta]
     double *e64;     // n_ent * 5
     double *t064;    // n_t0
     double *red;     // 33
-    float4 *e32a;    // n_ent
-    float2 *e32b;    // n_ent
-    float2 *t032;    // n_t0
+    float4 *e32a;    // [kGroup][n_ent]
+    float2 *e32b;    // [kGroup][n_ent]
+    float2 *t032;    // [kGroup][n_t0]
     uint8_t *cent;   // n_cell * n_acc
     uint8_t *cw;     // n_cell
     uint8_t *ct0;    // n_cell
-    int *flag;       // 4
+    int *flag;       // [kGroup] 1: FP32 form unusable for proposal g
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -284,19 +281,19 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 __host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[11])
 {
     size_t o = 0;
-    off[0] = o; o += sizeof(double) * kMaxTheta;
+    off[0] = o; o += sizeof(double) * kMaxTheta * kGroup;
     off[1] = o; o += sizeof(double) * 5 * m.n_ent;
     off[2] = o; o += sizeof(double) * m.n_t0;
     off[3] = o; o += sizeof(double) * 33;
     o = align_up(o, 16);
-    off[4] = o; o += sizeof(float4) * m.n_ent;
-    off[5] = o; o += sizeof(float2) * m.n_ent;
-    off[6] = o; o += sizeof(float2) * m.n_t0;
+    off[4] = o; o += sizeof(float4) * m.n_ent * kGroup;
+    off[5] = o; o += sizeof(float2) * m.n_ent * kGroup;
+    off[6] = o; o += sizeof(float2) * m.n_t0 * kGroup;
     off[7] = o; o += (size_t)m.n_cell * m.n_acc;
     off[8] = o; o += m.n_cell;
     off[9] = o; o += m.n_cell;
     o = align_up(o, 16);
-    off[10] = o; o += sizeof(int) * 4;
+    off[10] = o; o += sizeof(int) * kGroup;
     return align_up(o, 16);
 }
 
@@ -335,20 +332,20 @@ __device__ void load_design(const RunDev &r, SubSmem &sm)
     }
 }
 
-// FP64 tables of sm.theta: (A, b, v, s, Phi(v/s)) per tuple, t0 per source.
-__device__ void build_tables64(const RunDev &r, SubSmem &sm)
+// FP64 tables of theta: (A, b, v, s, Phi(v/s)) per tuple, t0 per source.
+__device__ void build_tables64(const RunDev &r, SubSmem &sm, const double *theta)
 {
     for (int u = threadIdx.x; u < r.m.n_ent; u += blockDim.x) {
         const EntSrc es = r.m.ent_src[u];
-        const double A = src_value(es.A, sm.theta, r.m.consts);
-        const double B = src_value(es.B, sm.theta, r.m.consts);
-        const double v = src_value(es.v, sm.theta, r.m.consts);
-        const double s = src_value(es.s, sm.theta, r.m.consts);
+        const double A = src_value(es.A, theta, r.m.consts);
+        const double B = src_value(es.B, theta, r.m.consts);
+        const double v = src_value(es.v, theta, r.m.consts);
+        const double s = src_value(es.s, theta, r.m.consts);
         double *e = sm.e64 + 5 * u;
         e[0] = A; e[1] = A + B; e[2] = v; e[3] = s; e[4] = Phi64(v / s);
     }
     for (int q = threadIdx.x; q < r.m.n_t0; q += blockDim.x)
-        sm.t064[q] = src_value(r.m.t0_src[q], sm.theta, r.m.consts);
+        sm.t064[q] = src_value(r.m.t0_src[q], theta, r.m.consts);
 }
 
 // FP32 table entry u of theta.  The exponent-sensitive ratios b/s, (b-A)/s
@@ -379,141 +376,189 @@ __device__ __forceinline__ float2 t0split(const RunDev &r, const double *theta, 
     return make_float2(hi, (float)(t0 - (double)hi));
 }
 
-// FP32 tables of sm.theta (sm.flag[0] = 1 when some tuple is outside the
-// FP32 form's domain).
-__device__ void build_tables32(const RunDev &r, SubSmem &sm)
+// FP32 tables of proposal g from sm.theta[g] (sets sm.flag[g]).
+__device__ void build_tables32(const RunDev &r, SubSmem &sm, int g)
 {
-    for (int u = threadIdx.x; u < r.m.n_ent; u += blockDim.x) {
+    const int NE = r.m.n_ent, NT = r.m.n_t0;
+    for (int u = threadIdx.x; u < NE; u += blockDim.x) {
         float4 a;
         float2 bb;
-        if (!entry32(r, sm.theta, u, a, bb)) sm.flag[0] = 1;
-        sm.e32a[u] = a;
-        sm.e32b[u] = bb;
+        if (!entry32(r, sm.theta + g * kMaxTheta, u, a, bb)) sm.flag[g] = 1;
+        sm.e32a[g * NE + u] = a;
+        sm.e32b[g * NE + u] = bb;
     }
-    for (int q = threadIdx.x; q < r.m.n_t0; q += blockDim.x) sm.t032[q] = t0split(r, sm.theta, q);
+    for (int q = threadIdx.x; q < NT; q += blockDim.x)
+        sm.t032[g * NT + q] = t0split(r, sm.theta + g * kMaxTheta, q);
 }
 
-// Tables of proposal `item`, as k_sub_propose / repropose stored them.
-__device__ void load_tables32(const RunDev &r, size_t item, SubSmem &sm)
+// Load proposal slot `slot` (theta and, in MIXED, its stored FP32 tables)
+// as group member g.
+__device__ void load_slot(const RunDev &r, size_t slot, SubSmem &sm, int g, bool mixed)
 {
-    for (int u = threadIdx.x; u < r.m.n_ent; u += blockDim.x) {
-        sm.e32a[u] = r.tab_a[item * r.m.n_ent + u];
-        sm.e32b[u] = r.tab_b[item * r.m.n_ent + u];
+    const int NE = r.m.n_ent, NT = r.m.n_t0;
+    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[g * kMaxTheta + j] = r.th_s[slot * r.P + j];
+    if (!mixed) return;
+    for (int u = threadIdx.x; u < NE; u += blockDim.x) {
+        sm.e32a[g * NE + u] = r.tab_a[slot * NE + u];
+        sm.e32b[g * NE + u] = r.tab_b[slot * NE + u];
     }
-    for (int q = threadIdx.x; q < r.m.n_t0; q += blockDim.x) sm.t032[q] = r.tab_t[item * r.m.n_t0 + q];
-    if (threadIdx.x == 0) sm.flag[0] = r.tab_bad[item];
+    for (int q = threadIdx.x; q < NT; q += blockDim.x) sm.t032[g * NT + q] = r.tab_t[slot * NT + q];
+    if (threadIdx.x == 0) sm.flag[g] = r.tab_bad[slot];
 }
 
-// Store the FP32 tables of proposal `item` (one thread).
-__device__ void store_tables(const RunDev &r, size_t item, const double *theta)
+// Trial log density of proposal g in FP64 (the reference form).
+__device__ __forceinline__ double trial64(const RunDev &r, const SubSmem &sm, int64_t gi, int c, int K)
 {
-    int bad = 0;
-    for (int u = 0; u < r.m.n_ent; ++u) {
-        float4 a;
-        float2 bb;
-        if (!entry32(r, theta, u, a, bb)) bad = 1;
-        r.tab_a[item * r.m.n_ent + u] = a;
-        r.tab_b[item * r.m.n_ent + u] = bb;
-    }
-    for (int q = 0; q < r.m.n_t0; ++q) r.tab_t[item * r.m.n_t0 + q] = t0split(r, theta, q);
-    r.tab_bad[item] = bad;
+    int e8[kMaxAcc];
+    for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
+    return lba_logdens64(r.rt64[gi] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c], sm.e64);
 }
 
-// Sum of per-trial log densities of subject level l at sm.theta on the whole
-// CTA (every thread gets the sum); sm.theta must be set and synchronised.
-// MIXED: FP32 first; the FP64 tables are built only when a trial of this CTA
-// needs the FP64 form, and only those trials use it.
-__device__ double sub_loglik_range(const RunDev &r, int l, int i0, int i1, SubSmem &sm, bool mixed,
-                                   bool tables_ready = false)
+// Log-likelihood sums over trials [i0, i1) of subject level l for the ng
+// (<= kGroup) proposals loaded in sm, on the whole CTA; out[g] valid on all
+// threads.  MIXED: FP32 per trial, each trial's data read once for the whole
+// group; FP64 tables are built only for a proposal some trial of which needs
+// the FP64 form, and only those trials use it.
+__device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed,
+                             double *out)
 {
     const int64_t base = r.offs[l] + i0;
     const int n = i1 - i0;
     const int K = r.m.n_acc;
-    bool fp64_all = !mixed;
-    if (mixed) {
-        if (!tables_ready) {
-            if (threadIdx.x == 0) sm.flag[0] = 0;
+    const int NE = r.m.n_ent, NT = r.m.n_t0;
+    if (!mixed) {
+        for (int g = 0; g < ng; ++g) {
+            build_tables64(r, sm, sm.theta + g * kMaxTheta);
             __syncthreads();
-            build_tables32(r, sm);
+            double acc = 0.0;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
+            out[g] = block_sum(acc, sm.red);
         }
-        __syncthreads();
-        fp64_all = sm.flag[0] != 0;
+        return;
     }
-    double acc64 = 0.0;
-    if (!fp64_all) {
-        float ks = 0.f, kc = 0.f;
-        int nfb = 0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int c = r.cell[base + i];
-            const float2 rt = r.rt32[base + i];
-            const float2 t0 = sm.t032[sm.ct0[c]];
+    __syncthreads();
+    bool ok[kGroup];
+    float ks[kGroup], kc[kGroup];
+    int nfb[kGroup];
+#pragma unroll
+    for (int g = 0; g < kGroup; ++g) {
+        ok[g] = g < ng && sm.flag[g] == 0;
+        ks[g] = 0.f; kc[g] = 0.f; nfb[g] = 0;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = r.cell[base + i];
+        const float2 rt = r.rt32[base + i];
+        const uint8_t *ents = sm.cent + c * K;
+        const int w = sm.cw[c], q0 = sm.ct0[c];
+#pragma unroll
+        for (int g = 0; g < kGroup; ++g) {
+            if (!ok[g]) continue;
+            const float2 t0 = sm.t032[g * NT + q0];
             const float t = (rt.x - t0.x) + (rt.y - t0.y);
             float ld;
-            if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a, sm.e32b, ld)) {
-                const float y = ld - kc;        // Kahan-compensated FP32 sum
-                const float tt = ks + y;
-                kc = (tt - ks) - y;
-                ks = tt;
+            if (lba_logdens32(t, ents, K, w, sm.e32a + g * NE, sm.e32b + g * NE, ld)) {
+                const float y = ld - kc[g];     // Kahan-compensated FP32 sum
+                const float tt = ks[g] + y;
+                kc[g] = (tt - ks[g]) - y;
+                ks[g] = tt;
             } else {
-                ++nfb;
+                ++nfb[g];
             }
         }
-        if (!__syncthreads_or(nfb > 0)) return block_sum_ff(ks, -kc, sm.red);
-        acc64 = (double)ks - (double)kc;
-        {
-            build_tables64(r, sm);
-            __syncthreads();
-            if (nfb > 0) {
-                for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                    const int c = r.cell[base + i];
+    }
+#pragma unroll
+    for (int g = 0; g < kGroup; ++g) {
+        if (g >= ng) break;
+        const bool usable = sm.flag[g] == 0;
+        if (!__syncthreads_or(nfb[g] > 0 || !usable)) {
+            out[g] = block_sum_ff(ks[g], -kc[g], sm.red);
+            continue;
+        }
+        build_tables64(r, sm, sm.theta + g * kMaxTheta);
+        __syncthreads();
+        double acc = usable ? (double)ks[g] - (double)kc[g] : 0.0;
+        if (!usable || nfb[g] > 0) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int c = r.cell[base + i];
+                if (usable) {
                     const float2 rt = r.rt32[base + i];
-                    const float2 t0 = sm.t032[sm.ct0[c]];
+                    const float2 t0 = sm.t032[g * NT + sm.ct0[c]];
                     const float t = (rt.x - t0.x) + (rt.y - t0.y);
                     float ld;
-                    if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a, sm.e32b, ld)) continue;
-                    int e8[kMaxAcc];
-                    for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
-                    acc64 += lba_logdens64(r.rt64[base + i] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c],
-                                           sm.e64);
+                    if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a + g * NE, sm.e32b + g * NE, ld))
+                        continue;
                 }
+                acc += trial64(r, sm, base + i, c, K);
             }
         }
-    } else {
-        build_tables64(r, sm);
+        out[g] = block_sum(acc, sm.red);
+    }
+}
+
+// Evaluate the log-likelihoods of proposal slots `slots[0..m)` of level l on
+// the whole CTA, kGroup at a time; results to ll_s (and to lls[k] when given).
+__device__ void eval_slots(const RunDev &r, int l, const int *slots, int m, SubSmem &sm, bool mixed,
+                           double *lls_sm)
+{
+    const int N = (int)(r.offs[l + 1] - r.offs[l]);
+    for (int g0 = 0; g0 < m; g0 += kGroup) {
+        const int ng = min(kGroup, m - g0);
+        for (int g = 0; g < ng; ++g) load_slot(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
         __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int c = r.cell[base + i];
-            int e8[kMaxAcc];
-            for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
-            acc64 += lba_logdens64(r.rt64[base + i] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c], sm.e64);
+        double out[kGroup];
+        group_loglik(r, l, 0, N, sm, ng, mixed, out);
+        if (threadIdx.x == 0) {
+            for (int g = 0; g < ng; ++g) {
+                r.ll_s[(size_t)l * r.CS + slots[g0 + g]] = out[g];
+                if (lls_sm) lls_sm[slots[g0 + g]] = out[g];
+            }
+            atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)N * ng);
         }
+        __syncthreads();
     }
-    return block_sum(acc64, sm.red);
 }
 
-__device__ __forceinline__ double sub_loglik_sum(const RunDev &r, int l, SubSmem &sm, bool mixed)
+// Store the FP32 tables of proposal slot `slot` from theta (threads of the
+// CTA in parallel over (slot, entry) are the caller's; this is one entry).
+__device__ __forceinline__ void store_entry(const RunDev &r, size_t slot, const double *theta, int u)
 {
-    return sub_loglik_range(r, l, 0, (int)(r.offs[l + 1] - r.offs[l]), sm, mixed);
+    const int NE = r.m.n_ent, NT = r.m.n_t0;
+    if (u < NE) {
+        float4 a;
+        float2 bb;
+        if (!entry32(r, theta, u, a, bb)) atomicOr(&r.tab_bad[slot], 1);
+        r.tab_a[slot * NE + u] = a;
+        r.tab_b[slot * NE + u] = bb;
+    } else {
+        r.tab_t[slot * NT + (u - NE)] = t0split(r, theta, u - NE);
+    }
 }
 
-// log-likelihood of proposal (l, k) on the whole CTA, written to ll_s
-__device__ void eval_item(const RunDev &r, int l, int k, SubSmem &sm, bool mixed)
+// One prior term of subject parameter j (fixed table or the truncated
+// normal of phi chain `owner`).
+__device__ __forceinline__ double prior_j(const RunDev &r, double x, int j, int owner)
 {
-    const size_t item = (size_t)l * r.C + k;
-    const double *th = r.th_s + item * r.P;
-    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
-    if (mixed) load_tables32(r, item, sm);
-    __syncthreads();
-    const double ll = sub_loglik_range(r, l, 0, (int)(r.offs[l + 1] - r.offs[l]), sm, mixed, mixed);
-    if (threadIdx.x == 0) {
-        r.ll_s[(size_t)l * r.C + k] = ll;
-        atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)(r.offs[l + 1] - r.offs[l]));
-    }
+    if (r.prior) return prior_term(r.prior + kPriorRow * j, x);
+    const double *pt = r.phi_tab + ((size_t)owner * r.P + j) * 3;   // (mu, 1/sigma, c)
+    if (x < r.pp_bounds[2 * j] || x > r.pp_bounds[2 * j + 1] || !(pt[1] > 0.0)) return -INFINITY;
+    const double z = (x - pt[0]) * pt[1];
+    return -0.5 * z * z + pt[2];
+}
+
+// Log prior of theta on one warp (lanes over parameters, fixed-order sum).
+__device__ __forceinline__ double warp_prior(const RunDev &r, const double *th, int owner)
+{
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    for (int j = lane; j < r.P; j += 32) s += prior_j(r, th[j], j, owner);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    return __shfl_sync(0xffffffffu, s, 0);
 }
 
 // --------------------------------------------------------- subject kernels
 // k_sub_propose: pass type, partners, stored draws and proposals of every
-// chain of every subject level, with their log priors.  grid = S.
+// chain of every subject level, with their log priors and FP32 tables.
+// grid = S.
 __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int pass)
 {
     __shared__ double s_u[kMaxChain + 2];
@@ -524,9 +569,7 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
     const int l = blockIdx.x;
     const int lev = r.level0 + l;
     const int64_t it = *r.iter;
-    const int C = r.C, P = r.P;
-    if (l == 0)
-        for (int q = threadIdx.x; q < r.n_round; q += blockDim.x) { r.qn[q] = 0; r.qc[q] = 0; }
+    const int C = r.C, P = r.P, CS = r.CS;
     if (threadIdx.x == 0) {
         int type = PASS_CROSS, para = -1;
         if (r.loop == LOOP_HCHAINS) {
@@ -548,8 +591,7 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
     __syncthreads();
     const int type = s_type, para = s_para;
     if (type == PASS_MIG) {
-        for (int q = 1 + threadIdx.x; q < C + 2; q += blockDim.x)
-            s_u[q] = uniform(r.ds, it, lev, pass, q);
+        for (int q = 1 + threadIdx.x; q < C + 2; q += blockDim.x) s_u[q] = uniform(r.ds, it, lev, pass, q);
         __syncthreads();
         if (threadIdx.x == 0) {
             s_n = subchains_from(C, s_u, s_sub, s_perm);
@@ -564,18 +606,11 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
         r.ptype[l] = type;
         r.nstep[l] = n;
         r.rs_para[l] = para;
-        r.rs_decided[l] = 0;
-        r.rs_done[l] = (n == 0) ? 1 : 0;
-    }
-    for (int k = threadIdx.x; k < C; k += blockDim.x) {
-        r.rs_mod[(size_t)l * C + k] = 0;
-        r.rs_ver[(size_t)l * C + k] = 0;
-        r.rs_pend[(size_t)l * C + k] = 0;
     }
     if (n == 0) return;
     const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
     const double *th = r.th + (size_t)l * C * P;
-    double *ths = r.th_s + (size_t)l * C * P;
+    double *ths = r.th_s + (size_t)l * CS * P;
     double *jit = r.jit + (size_t)l * C * P;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         if (type == PASS_CROSS) {
@@ -589,6 +624,7 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
             r.sub[(size_t)l * C + k] = s_sub[k];
         }
         r.accu[(size_t)l * C + k] = accept_draw(r, it, lev, pass, k);
+        r.tab_bad[(size_t)l * CS + k] = 0;
     }
     __syncthreads();
     // proposals, one thread per (step, parameter)
@@ -601,351 +637,396 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
             const double jv = jitter_draw(r, it, lev, pass, k, j);
             jit[(size_t)k * P + j] = jv;
             out = (type == PASS_CROSS)
-                      ? cross_comp(r.gamma, ts, th[(size_t)s_pa[k] * P + j],
-                                   th[(size_t)s_pb[k] * P + j], jv)
+                      ? cross_comp(r.gamma, ts, th[(size_t)s_pa[k] * P + j], th[(size_t)s_pb[k] * P + j], jv)
                       : __dadd_rn(ts, jv);
         }
         ths[(size_t)k * P + j] = out;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = wid; k < n; k += nw) {
         const int owner = (type == PASS_CROSS) ? k : s_sub[k];
-        const double lp = sub_prior(r, ths + (size_t)k * P, owner);
-        r.lp_s[(size_t)l * C + k] = lp;
-        r.ll_s[(size_t)l * C + k] = 0.0;
-        r.need[(size_t)l * C + k] = (lp > -INFINITY) ? 1 : 0;
-        r.tab_bad[(size_t)l * C + k] = 0;
-    }
-    if (r.prec != PREC_MIXED) return;
-    __syncthreads();
-    const int NE = r.m.n_ent, NT = r.m.n_t0;
-    for (int q = threadIdx.x; q < n * (NE + NT); q += blockDim.x) {
-        const int k = q / (NE + NT), u = q % (NE + NT);
-        const size_t item = (size_t)l * C + k;
-        if (u < NE) {
-            float4 a;
-            float2 bb;
-            if (!entry32(r, ths + (size_t)k * P, u, a, bb)) r.tab_bad[item] = 1;
-            r.tab_a[item * NE + u] = a;
-            r.tab_b[item * NE + u] = bb;
-        } else {
-            r.tab_t[item * NT + (u - NE)] = t0split(r, ths + (size_t)k * P, u - NE);
+        const double lp = warp_prior(r, ths + (size_t)k * P, owner);
+        if ((threadIdx.x & 31) == 0) {
+            r.lp_s[(size_t)l * CS + k] = lp;
+            r.ll_s[(size_t)l * CS + k] = 0.0;
+            r.need[(size_t)l * CS + k] = (lp > -INFINITY) ? 1 : 0;
         }
     }
+    // migration: the cascade V_s = V_(s-1) + jit_s from V_0 = proposal 0, the
+    // proposal step s gets when every step before it accepts (slots C + s)
+    const int nv = (type == PASS_MIG) ? n : 0;
+    for (int w = nv + threadIdx.x; w < C; w += blockDim.x) r.need[(size_t)l * CS + C + w] = 0;
+    if (nv) {
+        for (int j = threadIdx.x; j < P; j += blockDim.x) {
+            double v = th[(size_t)s_sub[0] * P + j];
+            for (int w = 0; w < nv; ++w) {
+                if (updated(j, para, nloop)) v = __dadd_rn(v, jit[(size_t)w * P + j]);
+                ths[(size_t)(C + w) * P + j] = v;
+            }
+        }
+        for (int w = threadIdx.x; w < nv; w += blockDim.x) r.tab_bad[(size_t)l * CS + C + w] = 0;
+        __syncthreads();
+        for (int w = wid; w < nv; w += nw) {
+            // V_0 equals proposal 0, already evaluated
+            const double lp = (w == 0) ? -INFINITY : warp_prior(r, ths + (size_t)(C + w) * P, s_sub[w]);
+            if ((threadIdx.x & 31) == 0) {
+                r.lp_s[(size_t)l * CS + C + w] = lp;
+                r.ll_s[(size_t)l * CS + C + w] = 0.0;
+                r.need[(size_t)l * CS + C + w] = (lp > -INFINITY) ? 1 : 0;
+            }
+        }
+    }
+    if (r.prec != PREC_MIXED) return;
+    const int NU = r.m.n_ent + r.m.n_t0;
+    for (int q = threadIdx.x; q < (n + nv) * NU; q += blockDim.x) {
+        const int k0 = q / NU, u = q % NU;
+        const int k = (k0 < n) ? k0 : C + (k0 - n);
+        store_entry(r, (size_t)l * CS + k, ths + (size_t)k * P, u);
+    }
 }
 
-// k_sub_loglik: the hot kernel.  One CTA per (level, step) item, items in
-// descending trial-count order (longest first keeps the tail short).
-__global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int32_t *items)
+// k_sub_loglik: the hot kernel.  One CTA per work item = up to kGroup
+// proposals of one subject, items in descending trial-count order (longest
+// first keeps the tail short).  item = level * CS + first slot.
+__global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int32_t *items, int group)
 {
     extern __shared__ __align__(16) char smem_raw[];
+    __shared__ int s_slots[kGroup];
+    __shared__ int s_m;
     const int32_t item = items[blockIdx.x];
-    const int l = item / r.C, k = item % r.C;
-    if (k >= r.nstep[l] || !r.need[(size_t)l * r.C + k]) return;
+    const int l = item / r.CS, k0 = item % r.CS;
+    const int n = r.nstep[l];
+    if (threadIdx.x == 0) {
+        int m = 0;
+        const int kend = (k0 < r.C) ? min(n, k0 + group) : min(r.C + n, k0 + group);
+        for (int k = k0; k < kend; ++k)
+            if (r.need[(size_t)l * r.CS + k]) s_slots[m++] = k;
+        s_m = m;
+    }
+    __syncthreads();
+    if (s_m == 0) return;
     SubSmem sm = carve(smem_raw, r.m);
     load_design(r, sm);
-    eval_item(r, l, k, sm, r.prec == PREC_MIXED);
+    eval_slots(r, l, s_slots, s_m, sm, r.prec == PREC_MIXED, nullptr);
 }
 
-// Working copy of one level's decision state in shared memory: the single
-// thread that takes the ordered decisions then touches no global memory.
-struct ScanSmem {
-    double *lp, *ll;       // [C] current state
-    double *lps, *lls;     // [n] proposals
-    double *accu;          // [n]
-    int *pa, *pb;          // [n] partners (crossover) / pa = subset (migration)
-    int16_t *ver;          // [n]
-    uint8_t *mod;          // [n]
-    uint8_t *flag;         // [n]
-    int *acc;              // [n] accepted steps of this scan
-    int *misc;             // [0] decided, [1] accepted count
+// Ordered decisions of one subject level per CTA (src/de.cpp:111-199,
+// 567-665).  Decisions are taken from the speculative results while the
+// proposal a step would get in sequence is the one evaluated; a
+// crossover chain whose partner moved earlier in the sweep is re-proposed
+// from the current state and re-evaluated with the other stale chains of
+// its round.  Migration steps: each round evaluates the next kVariants steps
+// as if the steps before them accept (a cascade carries one value forward);
+// after a rejection the next step's start-of-pass proposal is valid again.
+struct ResSmem {
+    double *lp, *ll;        // [C] current state
+    double *lps, *lls;      // [C] proposal values of each step
+    double *cur;            // [C] migration: log posterior of each step's destination
+    double *vlp, *vll;      // [C] migration variants
+    double *accu;           // [C]
+    int *pa, *pb;           // [C] partners (crossover) / pa = subset (migration)
+    int *acc, *accslot;     // [C] accepted steps of a scan and the slot they used
+    int *list;              // [C + kVariants] steps / slots to evaluate
+    int16_t *ver;           // [C]
+    uint8_t *mod, *flag, *dec;   // [C]
+    int *misc;              // 8
 };
 
-__host__ __device__ inline size_t scan_smem_bytes(int C)
+__host__ __device__ inline size_t res_smem_bytes(int C)
 {
-    return align_up((size_t)C * (5 * sizeof(double) + 3 * sizeof(int) + sizeof(int16_t) + 2) + 64, 16);
+    return align_up((size_t)C * (8 * sizeof(double) + 5 * sizeof(int) + sizeof(int16_t) + 3) +
+                        kVariants * sizeof(int) + 8 * sizeof(int) + 64, 16);
 }
 
-__device__ ScanSmem carve_scan(char *base, int C)
+__device__ ResSmem carve_res(char *base, int C)
 {
-    ScanSmem s;
+    ResSmem s;
     s.lp = (double *)base;
     s.ll = s.lp + C;
     s.lps = s.ll + C;
     s.lls = s.lps + C;
-    s.accu = s.lls + C;
-    s.pa = (int *)(s.accu + C);
+    s.cur = s.lls + C;
+    s.accu = s.cur + C;
+    s.vlp = s.accu + C;
+    s.vll = s.vlp + C;
+    s.pa = (int *)(s.vll + C);
     s.pb = s.pa + C;
     s.acc = s.pb + C;
-    s.misc = s.acc + C;
-    s.ver = (int16_t *)(s.misc + 4);
+    s.accslot = s.acc + C;
+    s.list = s.accslot + C;
+    s.misc = s.list + C + kVariants;
+    s.ver = (int16_t *)(s.misc + 8);
     s.mod = (uint8_t *)(s.ver + C);
     s.flag = s.mod + C;
+    s.dec = s.flag + C;
     return s;
 }
 
-// Sum the chunk partials of re-evaluations queued by the previous round
-// (fixed order, so the result does not depend on scheduling).
-__device__ void finalize_pending(const RunDev &r, int l, int n)
-{
-    const int64_t N = r.offs[l + 1] - r.offs[l];
-    const int nch = (int)((N + r.chunk - 1) / r.chunk);
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const size_t item = (size_t)l * r.C + k;
-        if (!r.rs_pend[item]) continue;
-        double s = 0.0;
-        for (int c = 0; c < nch; ++c) s += r.part[item * r.max_chunk + c];
-        r.ll_s[item] = s;
-        r.rs_pend[item] = 0;
-    }
-}
-
-// One ordered-decision pass over level l (all threads): load the state,
-// let thread 0 decide from the saved position while the speculative
-// proposals are valid, write the accepted rows back.  Returns the position.
-__device__ int decide(const RunDev &r, int l, int type, int n, ScanSmem &ss)
+// Copy the rows of the steps accepted by the last scan into the state.
+__device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na)
 {
     const int C = r.C, P = r.P;
-    const size_t lc = (size_t)l * C;
-    for (int k = threadIdx.x; k < C; k += blockDim.x) {
-        ss.lp[k] = r.lp[lc + k];
-        ss.ll[k] = r.ll[lc + k];
-    }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        ss.lps[k] = r.lp_s[lc + k];
-        ss.lls[k] = r.ll_s[lc + k];
-        ss.accu[k] = r.accu[lc + k];
-        ss.ver[k] = r.rs_ver[lc + k];
-        ss.mod[k] = r.rs_mod[lc + k];
-        if (type == PASS_CROSS) {
-            ss.pa[k] = r.partner[(lc + k) * 2];
-            ss.pb[k] = r.partner[(lc + k) * 2 + 1];
-        } else {
-            ss.pa[k] = r.sub[lc + k];
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int i = r.rs_decided[l], na = 0;
-        while (i < n) {
-            int dst;
-            if (type == PASS_CROSS) {
-                const int a = ss.pa[i], b = ss.pb[i], v = ss.ver[i];
-                if ((a >= v && a < i && ss.mod[a]) || (b >= v && b < i && ss.mod[b])) break;
-                dst = i;
-            } else {
-                if (i > 0 && ss.mod[i - 1] && ss.ver[i] < i) break;
-                dst = (i + 1 == n) ? ss.pa[0] : ss.pa[i + 1];
-            }
-            const double cur = (type == PASS_CROSS) ? ss.ll[dst] + ss.lp[dst] : ss.lp[dst] + ss.ll[dst];
-            bool ok = false;
-            if (mh_accept((ss.lps[i] + ss.lls[i]) - cur, ss.accu[i])) {
-                ss.lp[dst] = ss.lps[i];
-                ss.ll[dst] = ss.lls[i];
-                ss.acc[na++] = i;
-                ok = true;
-            }
-            ss.mod[i] = ok ? 1 : 0;
-            ++i;
-        }
-        ss.misc[0] = i;
-        ss.misc[1] = na;
-        r.rs_decided[l] = i;
-    }
-    __syncthreads();
-    const int d = ss.misc[0], na = ss.misc[1];
+    const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
     for (int q = threadIdx.x; q < na * P; q += blockDim.x) {
-        const int i = ss.acc[q / P], j = q % P;
-        const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? ss.pa[0] : ss.pa[i + 1]);
-        r.th[(lc + dst) * P + j] = r.th_s[(lc + i) * P + j];
+        const int a = q / P, j = q % P;
+        const int i = rs.acc[a];
+        const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? rs.pa[0] : rs.pa[i + 1]);
+        r.th[(lc + dst) * P + j] = r.th_s[(ls + rs.accslot[a]) * P + j];
     }
-    for (int q = threadIdx.x; q < na; q += blockDim.x) {
-        const int i = ss.acc[q];
-        const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? ss.pa[0] : ss.pa[i + 1]);
-        r.lp[lc + dst] = ss.lp[dst];
-        r.ll[lc + dst] = ss.ll[dst];
+    for (int a = threadIdx.x; a < na; a += blockDim.x) {
+        const int i = rs.acc[a];
+        const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? rs.pa[0] : rs.pa[i + 1]);
+        const int sl = rs.accslot[a];
+        const double lpv = (sl < C) ? rs.lps[sl] : rs.vlp[sl - C];
+        const double llv = (sl < C) ? rs.lls[sl] : rs.vll[sl - C];
+        r.lp[lc + dst] = lpv;
+        r.ll[lc + dst] = llv;
+        rs.lp[dst] = lpv;
+        rs.ll[dst] = llv;
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) r.rs_mod[lc + k] = ss.mod[k];
     if (threadIdx.x == 0 && na) atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)na);
     __syncthreads();
-    return d;
 }
 
-// Re-propose the steps of level l made stale by the decisions before
-// `decided`: for a crossover every later chain whose partner in
-// [ver, decided) moved (threads in parallel), for a migration step
-// `decided` (one thread).  flag[k] = 1 for each re-proposed step.
-__device__ void repropose(const RunDev &r, int l, int type, int n, int decided, uint8_t *flag)
-{
-    const int C = r.C, P = r.P;
-    const double *th = r.th + (size_t)l * C * P;
-    double *ths = r.th_s + (size_t)l * C * P;
-    const double *jit = r.jit + (size_t)l * C * P;
-    const int32_t *prt = r.partner + (size_t)l * C * 2;
-    const int32_t *sub = r.sub + (size_t)l * C;
-    const uint8_t *mod = r.rs_mod + (size_t)l * C;
-    int16_t *ver = r.rs_ver + (size_t)l * C;
-    const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
-    const int para = r.rs_para[l];
-    for (int k = threadIdx.x; k < n; k += blockDim.x) flag[k] = 0;
-    __syncthreads();
-    if (type == PASS_CROSS) {
-        for (int k = decided + (int)threadIdx.x; k < n; k += blockDim.x) {
-            const int a = prt[2 * k], b = prt[2 * k + 1];
-            const int v = ver[k];
-            const bool stale = (a >= v && a < decided && mod[a]) || (b >= v && b < decided && mod[b]);
-            ver[k] = (int16_t)decided;
-            if (stale) {
-                cross_prop_j(r.gamma, para, nloop, P, th + (size_t)k * P, th + (size_t)a * P,
-                             th + (size_t)b * P, jit + (size_t)k * P, ths + (size_t)k * P);
-                const double lpv = sub_prior(r, ths + (size_t)k * P, k);
-                r.lp_s[(size_t)l * C + k] = lpv;
-                r.ll_s[(size_t)l * C + k] = 0.0;
-                r.need[(size_t)l * C + k] = (lpv > -INFINITY) ? 1 : 0;
-                if (r.prec == PREC_MIXED && lpv > -INFINITY)
-                    store_tables(r, (size_t)l * C + k, ths + (size_t)k * P);
-                flag[k] = 1;
-            }
-        }
-    } else if (threadIdx.x == 0) {
-        const int k = decided;
-        mig_prop_j(para, nloop, P, th + (size_t)sub[k] * P, jit + (size_t)k * P, ths + (size_t)k * P);
-        const double lpv = sub_prior(r, ths + (size_t)k * P, sub[k]);
-        r.lp_s[(size_t)l * C + k] = lpv;
-        r.ll_s[(size_t)l * C + k] = 0.0;
-        r.need[(size_t)l * C + k] = (lpv > -INFINITY) ? 1 : 0;
-        if (r.prec == PREC_MIXED && lpv > -INFINITY)
-            store_tables(r, (size_t)l * C + k, ths + (size_t)k * P);
-        ver[k] = (int16_t)k;
-        flag[k] = 1;
-    }
-    __syncthreads();
-}
-
-// k_sub_round: one global round.  Per subject level (grid = S): sum the
-// previous round's partials, decide what can be decided, re-propose every
-// stale step and queue its trial chunks for k_sub_loglik_queue.
-__global__ void __launch_bounds__(kRoundThreads) k_sub_round(RunDev r, int pass, int round)
-{
-    extern __shared__ __align__(16) char smem_raw[];
-    const int l = blockIdx.x;
-    if (r.rs_done[l]) return;
-    ScanSmem ss = carve_scan(smem_raw, r.C);
-    const int type = r.ptype[l];
-    const int n = r.nstep[l];
-    finalize_pending(r, l, n);
-    __syncthreads();
-    const int decided = decide(r, l, type, n, ss);
-    if (threadIdx.x == 0) atomicAdd(&r.stats[ST_ROUNDS], 1ull);
-    if (decided >= n) {
-        if (threadIdx.x == 0) {
-            r.rs_done[l] = 1;
-            atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
-        }
-        return;
-    }
-    repropose(r, l, type, n, decided, ss.flag);
-    const int64_t N = r.offs[l + 1] - r.offs[l];
-    const int nch = (int)((N + r.chunk - 1) / r.chunk);
-    int32_t *q = r.queue + (size_t)round * r.S * r.C * r.max_chunk;
-    for (int k = decided + threadIdx.x; k < n; k += blockDim.x) {
-        if (!ss.flag[k]) continue;
-        atomicAdd(&r.stats[ST_REEVALS], 1ull);
-        const size_t item = (size_t)l * r.C + k;
-        if (!r.need[item] || nch == 0) continue;
-        for (int c = 0; c < nch; ++c) r.part[item * r.max_chunk + c] = 0.0;
-        r.rs_pend[item] = 1;
-        const int slot = atomicAdd(&r.qn[round], nch);
-        for (int c = 0; c < nch; ++c) q[slot + c] = (int32_t)(item * r.max_chunk + c);
-        atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)N);
-    }
-}
-
-// k_sub_loglik_queue: persistent CTAs take queued (proposal, trial chunk)
-// units (dynamic scheduling) and write each chunk's partial sum.
-__global__ void __launch_bounds__(kLikThreads) k_sub_loglik_queue(RunDev r, int round)
-{
-    extern __shared__ __align__(16) char smem_raw[];
-    __shared__ int s_unit;
-    const int nq = r.qn[round];
-    if (nq == 0) return;
-    SubSmem sm = carve(smem_raw, r.m);
-    load_design(r, sm);
-    const int32_t *q = r.queue + (size_t)round * r.S * r.C * r.max_chunk;
-    const bool mixed = r.prec == PREC_MIXED;
-    for (;;) {
-        if (threadIdx.x == 0) s_unit = atomicAdd(&r.qc[round], 1);
-        __syncthreads();
-        const int idx = s_unit;
-        if (idx >= nq) break;
-        const int unit = q[idx];
-        const int item = unit / r.max_chunk, c = unit % r.max_chunk;
-        const int l = item / r.C;
-        const double *th = r.th_s + (size_t)item * r.P;
-        for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
-        if (mixed) load_tables32(r, (size_t)item, sm);
-        __syncthreads();
-        const int N = (int)(r.offs[l + 1] - r.offs[l]);
-        const int i0 = c * r.chunk, i1 = min(N, i0 + r.chunk);
-        const double s = sub_loglik_range(r, l, i0, i1, sm, mixed, mixed);
-        if (threadIdx.x == 0) r.part[unit] = s;
-    }
-}
-
-// k_sub_resolve: finishes, within one CTA per subject, the decisions the
-// global rounds left (continuing from the saved position).
-__global__ void __launch_bounds__(kResolveThreads) k_sub_resolve(RunDev r, int pass, int level_begin)
+__global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, int pass, int level_begin)
 {
     extern __shared__ __align__(16) char smem_raw[];
     const int l = level_begin + blockIdx.x;
-    if (r.rs_done[l]) return;
     const int type = r.ptype[l];
+    if (type == PASS_SKIP) return;
     const int n = r.nstep[l];
+    const int C = r.C, P = r.P, CS = r.CS;
+    const size_t lc = (size_t)l * C, ls = (size_t)l * CS;
     const bool mixed = r.prec == PREC_MIXED;
     SubSmem sm = carve(smem_raw, r.m);
-    ScanSmem ss = carve_scan(smem_raw + sub_smem_bytes(r.m), r.C);
+    ResSmem rs = carve_res(smem_raw + sub_smem_bytes(r.m), C);
     load_design(r, sm);
-    finalize_pending(r, l, n);
+    for (int k = threadIdx.x; k < C; k += blockDim.x) {
+        rs.lp[k] = r.lp[lc + k];
+        rs.ll[k] = r.ll[lc + k];
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        rs.lps[k] = r.lp_s[ls + k];
+        rs.lls[k] = r.ll_s[ls + k];
+        rs.accu[k] = r.accu[lc + k];
+        rs.ver[k] = 0;
+        rs.mod[k] = 0;
+        if (type == PASS_CROSS) {
+            rs.pa[k] = r.partner[(lc + k) * 2];
+            rs.pb[k] = r.partner[(lc + k) * 2 + 1];
+        } else {
+            rs.pa[k] = r.sub[lc + k];
+        }
+    }
     __syncthreads();
-    int reevals = 0, rounds = 0;
+    const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
+    const int para = r.rs_para[l];
+    const double *jit = r.jit + lc * P;
+    int rounds = 0, reevals = 0, variants = 0;
+    int decided = 0;
 #ifdef GGDMC_PHASE_PROFILE
-    long long c_dec = 0, c_rep = 0, c_ev = 0, t_a;
+    long long c_dec = 0, c_rep = 0, c_ev = 0, t_a = 0, t_start = clock64();
 #define PH_T0() t_a = clock64()
 #define PH_ADD(x) x += clock64() - t_a
 #else
 #define PH_T0()
 #define PH_ADD(x)
 #endif
-    for (int round = 0; round <= n; ++round) {
-        ++rounds;
-        PH_T0();
-        const int decided = decide(r, l, type, n, ss);
-        PH_ADD(c_dec);
-        if (decided >= n) break;
-        PH_T0();
-        repropose(r, l, type, n, decided, ss.flag);
-        PH_ADD(c_rep);
-        PH_T0();
-        const int kend = (type == PASS_CROSS) ? n : decided + 1;
-        for (int k = decided; k < kend; ++k) {
-            if (!ss.flag[k]) continue;
-            ++reevals;
-            if (r.need[(size_t)l * r.C + k]) eval_item(r, l, k, sm, mixed);
+    if (type == PASS_CROSS) {
+        while (decided < n) {
+            ++rounds;
+            PH_T0();
+            // Metropolis outcome of every undecided step: it depends only on
+            // the step's own proposal and its own chain's current state.
+            for (int k = decided + threadIdx.x; k < n; k += blockDim.x)
+                rs.dec[k] = mh_accept((rs.lps[k] + rs.lls[k]) - (rs.ll[k] + rs.lp[k]), rs.accu[k]) ? 1 : 0;
             __syncthreads();
+            if (threadIdx.x == 0) {
+                int i = decided, na = 0;
+                while (i < n) {
+                    const int a = rs.pa[i], b = rs.pb[i], v = rs.ver[i];
+                    if ((a >= v && a < i && rs.mod[a]) || (b >= v && b < i && rs.mod[b])) break;
+                    rs.mod[i] = rs.dec[i];
+                    if (rs.dec[i]) { rs.acc[na] = i; rs.accslot[na] = i; ++na; }
+                    ++i;
+                }
+                rs.misc[0] = i;
+                rs.misc[1] = na;
+            }
+            __syncthreads();
+            const int d = rs.misc[0];
+            write_accepts(r, l, type, n, rs, rs.misc[1]);
+            decided = d;
+            PH_ADD(c_dec);
+            if (decided >= n) break;
+            PH_T0();
+            // stale chains: a partner in [ver, decided) moved
+            if (threadIdx.x == 0) {
+                int m = 0;
+                for (int k = decided; k < n; ++k) {
+                    const int a = rs.pa[k], b = rs.pb[k], v = rs.ver[k];
+                    if ((a >= v && a < decided && rs.mod[a]) || (b >= v && b < decided && rs.mod[b]))
+                        rs.list[m++] = k;
+                    rs.ver[k] = (int16_t)decided;
+                }
+                rs.misc[2] = m;
+            }
+            __syncthreads();
+            const int m = rs.misc[2];
+            reevals += m;
+            for (int q = threadIdx.x; q < m * P; q += blockDim.x) {
+                const int k = rs.list[q / P], j = q % P;
+                const double tk = r.th[(lc + k) * P + j];
+                r.th_s[(ls + k) * P + j] =
+                    updated(j, para, nloop)
+                        ? cross_comp(r.gamma, tk, r.th[(lc + rs.pa[k]) * P + j], r.th[(lc + rs.pb[k]) * P + j],
+                                     jit[(size_t)k * P + j])
+                        : tk;
+            }
+            for (int q = threadIdx.x; q < m; q += blockDim.x) r.tab_bad[ls + rs.list[q]] = 0;
+            __syncthreads();
+            const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            for (int q = wid; q < m; q += nw) {
+                const int k = rs.list[q];
+                const double lp = warp_prior(r, r.th_s + (ls + k) * P, k);
+                if ((threadIdx.x & 31) == 0) {
+                    rs.lps[k] = lp;
+                    rs.lls[k] = 0.0;
+                    r.lp_s[ls + k] = lp;
+                    r.ll_s[ls + k] = 0.0;
+                }
+            }
+            if (mixed) {
+                const int NU = r.m.n_ent + r.m.n_t0;
+                for (int q = threadIdx.x; q < m * NU; q += blockDim.x) {
+                    const int k = rs.list[q / NU];
+                    store_entry(r, ls + k, r.th_s + (ls + k) * P, q % NU);
+                }
+            }
+            __syncthreads();
+            // evaluate the re-proposed chains whose prior is finite
+            if (threadIdx.x == 0) {
+                int e = 0;
+                for (int q = 0; q < m; ++q)
+                    if (rs.lps[rs.list[q]] > -INFINITY) rs.list[e++] = rs.list[q];
+                rs.misc[3] = e;
+            }
+            __syncthreads();
+            PH_ADD(c_rep);
+            PH_T0();
+            eval_slots(r, l, rs.list, rs.misc[3], sm, mixed, rs.lls);
+            PH_ADD(c_ev);
         }
-        PH_ADD(c_ev);
+    } else {
+        // migration: cur[s] = log posterior of step s's destination, which
+        // only step s itself can change
+        for (int s = threadIdx.x; s < n; s += blockDim.x) {
+            const int dst = (s + 1 == n) ? rs.pa[0] : rs.pa[s + 1];
+            rs.cur[s] = rs.lp[dst] + rs.ll[dst];
+        }
+        __syncthreads();
+        for (int w = threadIdx.x; w < n; w += blockDim.x) {
+            rs.vlp[w] = r.lp_s[ls + C + w];
+            rs.vll[w] = r.ll_s[ls + C + w];
+        }
+        __syncthreads();
+        while (decided < n) {
+            ++rounds;
+            PH_T0();
+            const int d = decided;
+            const int nv = (d == 0) ? n : min(kVariants, n - d);
+            const bool spec0 = (d == 0) || !rs.mod[d - 1];   // step d's source is unchanged
+            if (d > 0) {
+            // variants: V_d = theta_src(d) + jit_d, V_s = V_(s-1) + jit_s
+            for (int j = threadIdx.x; j < P; j += blockDim.x) {
+                double v = r.th[(lc + rs.pa[d]) * P + j];
+                for (int w = 0; w < nv; ++w) {
+                    if (updated(j, para, nloop)) v = __dadd_rn(v, jit[(size_t)(d + w) * P + j]);
+                    r.th_s[(ls + C + w) * P + j] = v;
+                }
+            }
+            for (int w = threadIdx.x; w < nv; w += blockDim.x) r.tab_bad[ls + C + w] = 0;
+            __syncthreads();
+            const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            for (int w = wid; w < nv; w += nw) {
+                const double lp = warp_prior(r, r.th_s + (ls + C + w) * P, rs.pa[d + w]);
+                if ((threadIdx.x & 31) == 0) {
+                    rs.vlp[w] = lp;
+                    rs.vll[w] = 0.0;
+                }
+            }
+            if (mixed) {
+                const int NU = r.m.n_ent + r.m.n_t0;
+                for (int q = threadIdx.x; q < nv * NU; q += blockDim.x) {
+                    const int w = q / NU;
+                    store_entry(r, ls + C + w, r.th_s + (ls + C + w) * P, q % NU);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int e = 0;
+                for (int w = spec0 ? 1 : 0; w < nv; ++w)
+                    if (rs.vlp[w] > -INFINITY) rs.list[e++] = C + w;
+                rs.misc[3] = e;
+            }
+            __syncthreads();
+            const int ne = rs.misc[3];
+            variants += ne;
+            PH_ADD(c_rep);
+            PH_T0();
+            if (ne) {
+                eval_slots(r, l, rs.list, ne, sm, mixed, nullptr);
+                for (int q = threadIdx.x; q < ne; q += blockDim.x)
+                    rs.vll[rs.list[q] - C] = r.ll_s[ls + rs.list[q]];
+                __syncthreads();
+            }
+            }
+            PH_ADD(c_ev);
+            PH_T0();
+            if (threadIdx.x == 0) {
+                int s = d, na = 0;
+                bool run = true;
+                while (s < n) {
+                    int slot;
+                    double lpv, llv;
+                    if (s == d) {
+                        slot = spec0 ? s : C;
+                    } else if (run && s < d + nv) {
+                        slot = C + (s - d);
+                    } else if (!rs.mod[s - 1]) {
+                        slot = s;
+                    } else {
+                        break;
+                    }
+                    lpv = (slot < C) ? rs.lps[slot] : rs.vlp[slot - C];
+                    llv = (slot < C) ? rs.lls[slot] : rs.vll[slot - C];
+                    const bool ok = mh_accept((lpv + llv) - rs.cur[s], rs.accu[s]);
+                    rs.mod[s] = ok ? 1 : 0;
+                    if (ok) { rs.acc[na] = s; rs.accslot[na] = slot; ++na; }
+                    else run = false;
+                    ++s;
+                }
+                rs.misc[0] = s;
+                rs.misc[1] = na;
+            }
+            __syncthreads();
+            decided = rs.misc[0];
+            write_accepts(r, l, type, n, rs, rs.misc[1]);
+            PH_ADD(c_dec);
+        }
     }
 #ifdef GGDMC_PHASE_PROFILE
     if (threadIdx.x == 0 && *r.iter == 3)
-        printf("PHASE l=%d type=%d N=%d reevals=%d rounds=%d dec=%lld rep=%lld ev=%lld\n", l, type,
-               (int)(r.offs[l + 1] - r.offs[l]), reevals, rounds, c_dec, c_rep, c_ev);
+        printf("PHASE l=%d type=%d N=%d n=%d reevals=%d variants=%d rounds=%d dec=%lld rep=%lld ev=%lld tot=%lld\n",
+               l, type, (int)(r.offs[l + 1] - r.offs[l]), n, reevals, variants, rounds, c_dec, c_rep, c_ev,
+               clock64() - t_start);
 #endif
     if (threadIdx.x == 0) {
-        r.rs_done[l] = 1;
         atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
         atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
+        atomicAdd(&r.stats[ST_VARIANTS], (unsigned long long)variants);
         atomicAdd(&r.stats[ST_ROUNDS], (unsigned long long)rounds);
-        atomicAdd(&r.stats[ST_FINISH], 1ull);
     }
 }
 
@@ -1290,9 +1371,13 @@ __global__ void __launch_bounds__(kLikThreads) k_loglik_batch(RunDev r, const do
     const double *th = theta + ((size_t)l * n_theta + k) * r.P;
     for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
     load_design(r, sm);
+    if (threadIdx.x == 0) sm.flag[0] = 0;
     __syncthreads();
-    const double ll = sub_loglik_sum(r, l, sm, r.prec == PREC_MIXED);
-    if (threadIdx.x == 0) out[(size_t)l * n_theta + k] = ll;
+    const bool mixed = r.prec == PREC_MIXED;
+    if (mixed) build_tables32(r, sm, 0);
+    double ll[kGroup];
+    group_loglik(r, l, 0, (int)(r.offs[l + 1] - r.offs[l]), sm, 1, mixed, ll);
+    if (threadIdx.x == 0) out[(size_t)l * n_theta + k] = ll[0];
 }
 
 // per-trial log densities of theta [S][P] -> out [N]; grid = S.
@@ -1307,8 +1392,8 @@ __global__ void __launch_bounds__(kLikThreads) k_trial_logdens(RunDev r, const d
     if (threadIdx.x == 0) sm.flag[0] = 0;
     __syncthreads();
     const bool mixed = r.prec == PREC_MIXED;
-    if (mixed) build_tables32(r, sm);
-    build_tables64(r, sm);
+    if (mixed) build_tables32(r, sm, 0);
+    build_tables64(r, sm, sm.theta);
     __syncthreads();
     const int64_t base = r.offs[l];
     const int n = (int)(r.offs[l + 1] - base);
@@ -1326,9 +1411,7 @@ __global__ void __launch_bounds__(kLikThreads) k_trial_logdens(RunDev r, const d
                 continue;
             }
         }
-        int e8[kMaxAcc];
-        for (int k = 0; k < K; ++k) e8[k] = sm.cent[c * K + k];
-        out[base + i] = lba_logdens64(r.rt64[base + i] - sm.t064[sm.ct0[c]], e8, K, sm.cw[c], sm.e64);
+        out[base + i] = trial64(r, sm, base + i, c, K);
     }
 }
 
@@ -1362,14 +1445,8 @@ cudaError_t configure_kernels(const DevModel &m)
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_sub_loglik, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
-    if ((e = cudaFuncSetAttribute(k_sub_loglik_queue, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  bytes)))
-        return e;
     if ((e = cudaFuncSetAttribute(k_sub_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  bytes + (int)scan_smem_bytes(kMaxChain))))
-        return e;
-    if ((e = cudaFuncSetAttribute(k_sub_round, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)scan_smem_bytes(kMaxChain))))
+                                  bytes + (int)res_smem_bytes(kMaxChain))))
         return e;
     if ((e = cudaFuncSetAttribute(k_loglik_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
@@ -1382,28 +1459,17 @@ cudaError_t launch_sub_propose(const RunDev &r, int pass, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, cudaStream_t st)
+cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, int group,
+                              cudaStream_t st)
 {
-    k_sub_loglik<<<n_items, kLikThreads, sub_smem_bytes(r.m), st>>>(r, items);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_sub_round(const RunDev &r, int pass, int round, cudaStream_t st)
-{
-    k_sub_round<<<r.S, kRoundThreads, scan_smem_bytes(r.C), st>>>(r, pass, round);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_sub_loglik_queue(const RunDev &r, int round, int n_blocks, cudaStream_t st)
-{
-    k_sub_loglik_queue<<<n_blocks, kLikThreads, sub_smem_bytes(r.m), st>>>(r, round);
+    k_sub_loglik<<<n_items, kLikThreads, sub_smem_bytes(r.m), st>>>(r, items, group);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
                                cudaStream_t st)
 {
-    k_sub_resolve<<<level_count, kResolveThreads, sub_smem_bytes(r.m) + scan_smem_bytes(r.C), st>>>(
+    k_sub_resolve<<<level_count, kResolveThreads, sub_smem_bytes(r.m) + res_smem_bytes(r.C), st>>>(
         r, pass, level_begin);
     return cudaGetLastError();
 }

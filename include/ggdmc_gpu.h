@@ -139,7 +139,7 @@ typedef struct {
     int64_t iterations;        /* DE iterations (sweeps) run    */
     double sweep_ms;           /* device time of the sweeps (CUDA events), ms */
     int64_t resolve_rounds;    /* ordered-decision rounds over all subject passes */
-    int64_t resolve_finish;    /* subject passes finished by the in-CTA resolve */
+    int64_t variants;          /* migration steps evaluated ahead of their decision */
 } ggdmc_run_stats;
 
 typedef struct ggdmc_handle ggdmc_handle;
