@@ -117,6 +117,26 @@ __device__ __forceinline__ double tnorm_const(double mu, double sigma, double lo
     return -0.91893853320467274178 - log(sigma) - log(mass);
 }
 
+// The same constant in FP32 (MIXED): on this GPU an FP64 erfc costs about
+// 4,300 cycles and an FP64 log about 2,000, and the constant is needed for
+// every phi vector scored.  The relative error of the FP32 form is ~1e-7.
+__device__ __forceinline__ double tnorm_const_mixed(double mu, double sigma, double lo, double hi)
+{
+    if (!(sigma > 0.0)) return -INFINITY;
+    const float is = 1.f / (float)sigma;
+    const float a = (float)(lo - mu) * is, b = (float)(hi - mu) * is;
+    float mass;
+    if (isinf(hi) && hi > 0) mass = 0.5f * erfcf(a * 0.70710678f);
+    else if (isinf(lo) && lo < 0) mass = 0.5f * erfcf(-b * 0.70710678f);
+    else mass = normcdff(b) - normcdff(a);
+    return (double)(-0.918938533f - logf((float)sigma) - logf(mass));
+}
+
+__device__ __forceinline__ double tnorm_const_p(const RunDev &r, double mu, double sigma, double lo, double hi)
+{
+    return (r.prec == PREC_MIXED) ? tnorm_const_mixed(mu, sigma, lo, hi) : tnorm_const(mu, sigma, lo, hi);
+}
+
 // Subject-level prior: fixed table, or the truncated normal of phi chain
 // `phi_chain` (src/de.cpp:599-603, 646-652).
 __device__ double sub_prior(const RunDev &r, const double *th, int phi_chain)
@@ -1040,7 +1060,7 @@ __device__ double hyper_sum(const RunDev &r, const double *phv, int chain, doubl
     // cst[p] = constant of the log density, cst[P + p] = 1 / sigma
     const int P = r.Pphi / 2;
     for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        cst[p] = tnorm_const(phv[p], phv[P + p], r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
+        cst[p] = tnorm_const_p(r, phv[p], phv[P + p], r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
         cst[P + p] = 1.0 / phv[P + p];
     }
     __syncthreads();
@@ -1188,24 +1208,76 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_eval(RunDev r)
     }
 }
 
-__device__ double phi_reeval(const RunDev &r, const double *vec, int chain, double *s_phi,
-                             double *s_cst, double *s_red)
+// Hyper log-likelihoods of m phi vectors at once, one warp per vector
+// (lanes over subject x parameter terms, fixed-order sums).  vecs[q] points
+// to vector q, chains[q] is the subject chain it is scored against; cst is
+// shared memory for 2 * m * P doubles.  Results to out[q].
+__device__ void phi_batch_hyper(const RunDev &r, const double *const *vecs, const int *chains, int m,
+                                double *cst, double *out)
 {
-    for (int j = threadIdx.x; j < r.Pphi; j += blockDim.x) s_phi[j] = vec[j];
+    const int P = r.Pphi / 2;
+    for (int t = threadIdx.x; t < m * P; t += blockDim.x) {
+        const int q = t / P, p = t % P;
+        const double mu = vecs[q][p], sg = vecs[q][P + p];
+        cst[2 * t] = tnorm_const_p(r, mu, sg, r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
+        cst[2 * t + 1] = (sg > 0.0) ? 1.0 / sg : 0.0;
+    }
     __syncthreads();
-    return hyper_sum(r, s_phi, chain, s_cst, s_red);
+    const int nrow = r.hrows ? r.n_row : r.S;
+    const bool fp32 = r.prec == PREC_MIXED;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = wid; q < m; q += nw) {
+        const double *v = vecs[q];
+        const double *cq = cst + 2 * q * P;
+        bool out_of_support = false;
+        double acc = 0.0;
+        float ks = 0.f, kc = 0.f;
+        // lanes over subjects; each subject's P parameters are contiguous
+        for (int sj = lane; sj < nrow; sj += 32) {
+            const double *xs = r.hrows ? r.hrows + (size_t)sj * P
+                                       : r.th + ((size_t)sj * r.C + chains[q]) * r.P;
+            for (int p = 0; p < P; ++p) {
+                const double x = xs[p];
+                if (x < r.pp_bounds[2 * p] || x > r.pp_bounds[2 * p + 1] || !(cq[2 * p + 1] > 0.0)) {
+                    out_of_support = true;
+                } else if (fp32) {
+                    const float z = (float)(x - v[p]) * (float)cq[2 * p + 1];
+                    const float term = fmaf(-0.5f * z, z, (float)cq[2 * p]);
+                    const float y = term - kc;
+                    const float tt = ks + y;
+                    kc = (tt - ks) - y;
+                    ks = tt;
+                } else {
+                    const double z = (x - v[p]) * cq[2 * p + 1];
+                    acc += -0.5 * z * z + cq[2 * p];
+                }
+            }
+        }
+        acc += (double)ks - (double)kc;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        const bool oos = __any_sync(0xffffffffu, out_of_support);
+        if (lane == 0) out[q] = oos ? -INFINITY : acc;
+    }
+    __syncthreads();
 }
 
-// k_phi_resolve: ordered decisions of the phi level (src/de.cpp:385-565).
-__global__ void __launch_bounds__(kPhiThreads) k_phi_resolve(RunDev r, int pass)
+// k_phi_resolve: ordered decisions of the phi level (src/de.cpp:385-565;
+// run_hyper's level follows src/de.cpp:111-199).  One CTA.
+constexpr int kPhiResolveThreads = 1024;
+constexpr int kPhiBatch = 16;       // phi vectors scored per batch
+
+__global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, int pass)
 {
-    __shared__ uint8_t s_mod[kMaxChain];
+    __shared__ double s_lps[kMaxChain], s_lls[kMaxChain], s_ref[kMaxChain];
+    __shared__ uint8_t s_mod[kMaxChain], s_dec[kMaxChain];
     __shared__ int16_t s_ver[kMaxChain];
-    __shared__ uint8_t s_flag[kMaxChain];
-    __shared__ double s_phi[kMaxTheta];
-    __shared__ double s_cst[2 * kMaxTheta];
-    __shared__ double s_red[33];
-    __shared__ int s_decided, s_acc;
+    __shared__ int s_list[kMaxChain], s_acc[kMaxChain];
+    __shared__ int16_t s_pa[kMaxChain], s_pb[kMaxChain];
+    __shared__ double s_cst[kPhiBatch * kMaxTheta];
+    __shared__ const double *s_vecs[kPhiBatch];
+    __shared__ int s_chains[kPhiBatch];
+    __shared__ double s_out[kPhiBatch];
+    __shared__ int s_misc[4];
     const int type = r.pptype[0];
     if (type == PASS_SKIP) return;
     const int C = r.C, P = r.Pphi;
@@ -1215,98 +1287,183 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_resolve(RunDev r, int pass)
     int para;
     if (r.phi_loop == LOOP_HCHAINS) para = r.phi_blocked ? pass : -1;
     else para = (type == PASS_MIG) ? -1 : (r.phi_blocked ? pass : -1);
-    for (int k = threadIdx.x; k < C; k += blockDim.x) { s_mod[k] = 0; s_ver[k] = 0; s_flag[k] = 0; }
-    if (threadIdx.x == 0) { s_decided = 0; s_acc = 0; }
-    __syncthreads();
-    int reevals = 0;
-    for (int round = 0; round <= n; ++round) {
-        if (threadIdx.x == 0) {
-            int i = s_decided;
-            while (i < n) {
-                int dst;
-                if (type == PASS_CROSS) {
-                    const int a = r.ppartner[2 * i], b = r.ppartner[2 * i + 1];
-                    const int v = s_ver[i];
+    int reevals = 0, accepts = 0;
+#ifdef GGDMC_PHASE_PROFILE
+    long long c_dec = 0, c_rep = 0, c_ev = 0, t_a = 0, t_start = clock64();
+    int nround = 0;
+#endif
+    if (type == PASS_CROSS) {
+        for (int k = threadIdx.x; k < C; k += blockDim.x) {
+            s_pa[k] = (int16_t)r.ppartner[2 * k];
+            s_pb[k] = (int16_t)r.ppartner[2 * k + 1];
+            s_lps[k] = r.plp_s[k];
+            s_lls[k] = r.pll_s[k];
+            // the refreshed hyper log-likelihood of chain k (src/de.cpp:397-400)
+            s_ref[k] = refresh ? r.pref_src[k] : r.pll[k];
+            s_ver[k] = 0;
+            s_mod[k] = 0;
+        }
+        __syncthreads();
+        int decided = 0;
+        while (decided < n) {
+#ifdef GGDMC_PHASE_PROFILE
+            ++nround;
+            t_a = clock64();
+#endif
+            for (int k = decided + threadIdx.x; k < n; k += blockDim.x)
+                s_dec[k] = mh_accept((s_lps[k] + s_lls[k]) - (s_ref[k] + r.plp[k]), r.paccu[k]) ? 1 : 0;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int i = decided, na = 0;
+                while (i < n) {
+                    const int a = s_pa[i], b = s_pb[i], v = s_ver[i];
                     if ((a >= v && a < i && s_mod[a]) || (b >= v && b < i && s_mod[b])) break;
-                    dst = i;
-                    if (refresh) r.pll[i] = r.pref_src[i];
-                } else {
-                    if (i > 0 && s_mod[i - 1] && s_ver[i] < i) break;
-                    const int src = r.psub[i];
-                    dst = (i + 1 == n) ? r.psub[0] : r.psub[i + 1];
-                    if (refresh) {
-                        r.pll[src] = r.pref_src[i];
-                        r.pll[dst] = r.pref_next[i];
-                    }
+                    s_mod[i] = s_dec[i];
+                    if (s_dec[i]) s_acc[na++] = i;
+                    ++i;
                 }
-                const double cur = (type == PASS_CROSS) ? r.pll[dst] + r.plp[dst]
-                                                        : r.plp[dst] + r.pll[dst];
-                bool ok = false;
-                if (mh_accept((r.plp_s[i] + r.pll_s[i]) - cur, r.paccu[i])) {
-                    for (int j = 0; j < P; ++j) r.pth[(size_t)dst * P + j] = r.pth_s[(size_t)i * P + j];
+                s_misc[0] = i;
+                s_misc[1] = na;
+            }
+            __syncthreads();
+            const int d = s_misc[0], na = s_misc[1];
+            accepts += na;
+            // decided steps: the refresh is stored, an accept overwrites it
+            for (int k = decided + threadIdx.x; k < d; k += blockDim.x) {
+                r.pll[k] = s_mod[k] ? s_lls[k] : s_ref[k];
+                if (s_mod[k]) r.plp[k] = s_lps[k];
+            }
+            for (int q = threadIdx.x; q < na * P; q += blockDim.x) {
+                const int i = s_acc[q / P], j = q % P;
+                r.pth[(size_t)i * P + j] = r.pth_s[(size_t)i * P + j];
+            }
+            decided = d;
+            __syncthreads();
+#ifdef GGDMC_PHASE_PROFILE
+            c_dec += clock64() - t_a;
+            t_a = clock64();
+#endif
+            if (decided >= n) break;
+            if (threadIdx.x == 0) {
+                int m = 0;
+                for (int k = decided; k < n; ++k) {
+                    const int a = s_pa[k], b = s_pb[k], v = s_ver[k];
+                    if ((a >= v && a < decided && s_mod[a]) || (b >= v && b < decided && s_mod[b]))
+                        s_list[m++] = k;
+                    s_ver[k] = (int16_t)decided;
+                }
+                s_misc[2] = m;
+            }
+            __syncthreads();
+            const int m = s_misc[2];
+            reevals += m;
+            for (int q = threadIdx.x; q < m * P; q += blockDim.x) {
+                const int k = s_list[q / P], j = q % P;
+                const double tk = r.pth[(size_t)k * P + j];
+                r.pth_s[(size_t)k * P + j] =
+                    updated(j, para, nloop)
+                        ? cross_comp(r.gamma, tk, r.pth[(size_t)s_pa[k] * P + j],
+                                     r.pth[(size_t)s_pb[k] * P + j], r.pjit[(size_t)k * P + j])
+                        : tk;
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < m; q += blockDim.x) {
+                const int k = s_list[q];
+                s_lps[k] = phi_prior(r, r.pth_s + (size_t)k * P);
+                s_lls[k] = 0.0;
+            }
+            __syncthreads();
+#ifdef GGDMC_PHASE_PROFILE
+            c_rep += clock64() - t_a;
+            t_a = clock64();
+#endif
+            for (int q0 = 0; q0 < m; q0 += kPhiBatch) {
+                const int mb = min(kPhiBatch, m - q0);
+                if (threadIdx.x < mb) {
+                    const int k = s_list[q0 + threadIdx.x];
+                    s_vecs[threadIdx.x] = r.pth_s + (size_t)k * P;
+                    s_chains[threadIdx.x] = k;
+                }
+                __syncthreads();
+                phi_batch_hyper(r, s_vecs, s_chains, mb, s_cst, s_out);
+                for (int q = threadIdx.x; q < mb; q += blockDim.x) {
+                    const int k = s_list[q0 + q];
+                    if (s_lps[k] > -INFINITY) s_lls[k] = s_out[q];
+                }
+                __syncthreads();
+            }
+            for (int q = threadIdx.x; q < m; q += blockDim.x) {
+                const int k = s_list[q];
+                r.plp_s[k] = s_lps[k];
+                r.pll_s[k] = s_lls[k];
+            }
+            __syncthreads();
+#ifdef GGDMC_PHASE_PROFILE
+            c_ev += clock64() - t_a;
+#endif
+        }
+#ifdef GGDMC_PHASE_PROFILE
+        if (threadIdx.x == 0)
+            printf("PHIPHASE it=%d n=%d rounds=%d reevals=%d accepts=%d dec=%lld rep=%lld ev=%lld tot=%lld\n",
+                   (int)*r.iter, n, nround, reevals, accepts, c_dec, c_rep, c_ev, clock64() - t_start);
+#endif
+    } else {
+        // migration (pop_migration_prob per sweep): steps in order; a step
+        // whose source was replaced by the previous step's accept is
+        // re-proposed from it, and its source's refreshed value recomputed.
+        if (threadIdx.x == 0) s_misc[0] = 0;
+        __syncthreads();
+        for (int i = 0; i < n; ++i) {
+            const int src = r.psub[i];
+            const int dst = (i + 1 == n) ? r.psub[0] : r.psub[i + 1];
+            const bool stale = i > 0 && s_misc[0];
+            if (stale) {
+                for (int j = threadIdx.x; j < P; j += blockDim.x)
+                    r.pth_s[(size_t)i * P + j] = updated(j, para, nloop)
+                        ? __dadd_rn(r.pth[(size_t)src * P + j], r.pjit[(size_t)i * P + j])
+                        : r.pth[(size_t)src * P + j];
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    s_vecs[0] = r.pth_s + (size_t)i * P;
+                    s_vecs[1] = r.pth + (size_t)src * P;
+                    s_chains[0] = src;
+                    s_chains[1] = src;
+                    s_lps[0] = phi_prior(r, r.pth_s + (size_t)i * P);
+                }
+                __syncthreads();
+                phi_batch_hyper(r, s_vecs, s_chains, refresh ? 2 : 1, s_cst, s_out);
+                if (threadIdx.x == 0) {
+                    r.plp_s[i] = s_lps[0];
+                    r.pll_s[i] = (s_lps[0] > -INFINITY) ? s_out[0] : 0.0;
+                    if (refresh) r.pref_src[i] = s_out[1];
+                }
+                ++reevals;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (refresh) {
+                    r.pll[src] = r.pref_src[i];
+                    r.pll[dst] = r.pref_next[i];
+                }
+                const double cur = r.plp[dst] + r.pll[dst];
+                const bool ok = mh_accept((r.plp_s[i] + r.pll_s[i]) - cur, r.paccu[i]);
+                if (ok) {
                     r.plp[dst] = r.plp_s[i];
                     r.pll[dst] = r.pll_s[i];
-                    ok = true;
-                    ++s_acc;
+                    ++accepts;
                 }
-                s_mod[i] = ok ? 1 : 0;
-                ++i;
+                s_misc[0] = ok ? 1 : 0;
             }
-            s_decided = i;
-        }
-        __syncthreads();
-        const int decided = s_decided;
-        if (decided >= n) break;
-        if (type == PASS_CROSS) {
-            for (int k = decided + threadIdx.x; k < n; k += blockDim.x) {
-                const int a = r.ppartner[2 * k], b = r.ppartner[2 * k + 1];
-                const int v = s_ver[k];
-                const bool stale = (a >= v && a < decided && s_mod[a]) ||
-                                   (b >= v && b < decided && s_mod[b]);
-                s_ver[k] = (int16_t)decided;
-                s_flag[k] = stale ? 1 : 0;
-                if (stale) {
-                    cross_prop_j(r.gamma, para, nloop, P, r.pth + (size_t)k * P, r.pth + (size_t)a * P,
-                                 r.pth + (size_t)b * P, r.pjit + (size_t)k * P,
-                                 r.pth_s + (size_t)k * P);
-                    const double lp = phi_prior(r, r.pth_s + (size_t)k * P);
-                    r.plp_s[k] = lp;
-                    r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
-                    r.pll_s[k] = 0.0;
-                }
-            }
-        } else if (threadIdx.x == 0) {
-            const int k = decided;
-            mig_prop_j(para, nloop, P, r.pth + (size_t)r.psub[k] * P, r.pjit + (size_t)k * P,
-                       r.pth_s + (size_t)k * P);
-            const double lp = phi_prior(r, r.pth_s + (size_t)k * P);
-            r.plp_s[k] = lp;
-            r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
-            r.pll_s[k] = 0.0;
-            s_ver[k] = (int16_t)k;
-            s_flag[k] = 1;
-        }
-        __syncthreads();
-        const int kend = (type == PASS_CROSS) ? n : decided + 1;
-        for (int k = decided; k < kend; ++k) {
-            if (!s_flag[k]) continue;
-            const int chain = (type == PASS_CROSS) ? k : r.psub[k];
-            double h = 0.0;
-            if (r.pneed[k]) h = phi_reeval(r, r.pth_s + (size_t)k * P, chain, s_phi, s_cst, s_red);
-            if (type == PASS_MIG && refresh) {
-                const double hs = phi_reeval(r, r.pth + (size_t)chain * P, chain, s_phi, s_cst, s_red);
-                if (threadIdx.x == 0) r.pref_src[k] = hs;
-            }
-            if (threadIdx.x == 0) r.pll_s[k] = h;
             __syncthreads();
-            ++reevals;
+            if (s_misc[0])
+                for (int j = threadIdx.x; j < P; j += blockDim.x)
+                    r.pth[(size_t)dst * P + j] = r.pth_s[(size_t)i * P + j];
+            __syncthreads();
         }
-        for (int k = decided + threadIdx.x; k < kend; k += blockDim.x) s_flag[k] = 0;
-        __syncthreads();
     }
     if (threadIdx.x == 0) {
         atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
-        atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)s_acc);
+        atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)accepts);
         atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
     }
 }
@@ -1322,7 +1479,7 @@ __global__ void k_phi_tables(RunDev r)
         double *o = r.phi_tab + ((size_t)i * P + p) * 3;
         o[0] = mu;
         o[1] = (sg > 0.0) ? 1.0 / sg : 0.0;     // 0 marks an invalid scale
-        o[2] = tnorm_const(mu, sg, r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
+        o[2] = tnorm_const_p(r, mu, sg, r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
     }
 }
 
@@ -1494,7 +1651,7 @@ cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st)
 
 cudaError_t launch_phi_resolve(const RunDev &r, int pass, cudaStream_t st)
 {
-    k_phi_resolve<<<1, kPhiThreads, 0, st>>>(r, pass);
+    k_phi_resolve<<<1, kPhiResolveThreads, 0, st>>>(r, pass);
     return cudaGetLastError();
 }
 
