@@ -1208,12 +1208,15 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_eval(RunDev r)
     }
 }
 
-// Hyper log-likelihoods of m phi vectors at once, one warp per vector
-// (lanes over subject x parameter terms, fixed-order sums).  vecs[q] points
-// to vector q, chains[q] is the subject chain it is scored against; cst is
-// shared memory for 2 * m * P doubles.  Results to out[q].
+// Hyper log-likelihoods of m phi vectors at once.  A round re-scores only a
+// few vectors, so every vector's subject x parameter terms are spread over
+// the whole block (a handful of independent loads per thread) rather than a
+// warp walking each subject's row in series; warp partials land in part[q][w]
+// and are summed in warp order.  vecs[q] points to vector q, chains[q] is the
+// subject chain it is scored against; cst holds 2 * m * P doubles, part
+// m * 32 doubles, oos m ints.  Results to out[q].
 __device__ void phi_batch_hyper(const RunDev &r, const double *const *vecs, const int *chains, int m,
-                                double *cst, double *out)
+                                double *cst, double *part, int *oos, double *out)
 {
     const int P = r.Pphi / 2;
     for (int t = threadIdx.x; t < m * P; t += blockDim.x) {
@@ -1222,41 +1225,46 @@ __device__ void phi_batch_hyper(const RunDev &r, const double *const *vecs, cons
         cst[2 * t] = tnorm_const_p(r, mu, sg, r.pp_bounds[2 * p], r.pp_bounds[2 * p + 1]);
         cst[2 * t + 1] = (sg > 0.0) ? 1.0 / sg : 0.0;
     }
+    if (threadIdx.x < m) oos[threadIdx.x] = 0;
     __syncthreads();
     const int nrow = r.hrows ? r.n_row : r.S;
+    const int nterm = nrow * P;
     const bool fp32 = r.prec == PREC_MIXED;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int q = wid; q < m; q += nw) {
+    for (int q = 0; q < m; ++q) {
         const double *v = vecs[q];
         const double *cq = cst + 2 * q * P;
-        bool out_of_support = false;
+        const size_t cbase = (size_t)chains[q] * r.P;
+        bool bad = false;
         double acc = 0.0;
-        float ks = 0.f, kc = 0.f;
-        // lanes over subjects; each subject's P parameters are contiguous
-        for (int sj = lane; sj < nrow; sj += 32) {
-            const double *xs = r.hrows ? r.hrows + (size_t)sj * P
-                                       : r.th + ((size_t)sj * r.C + chains[q]) * r.P;
-            for (int p = 0; p < P; ++p) {
-                const double x = xs[p];
-                if (x < r.pp_bounds[2 * p] || x > r.pp_bounds[2 * p + 1] || !(cq[2 * p + 1] > 0.0)) {
-                    out_of_support = true;
-                } else if (fp32) {
-                    const float z = (float)(x - v[p]) * (float)cq[2 * p + 1];
-                    const float term = fmaf(-0.5f * z, z, (float)cq[2 * p]);
-                    const float y = term - kc;
-                    const float tt = ks + y;
-                    kc = (tt - ks) - y;
-                    ks = tt;
-                } else {
-                    const double z = (x - v[p]) * cq[2 * p + 1];
-                    acc += -0.5 * z * z + cq[2 * p];
-                }
+        float facc = 0.f;
+        for (int e = threadIdx.x; e < nterm; e += blockDim.x) {
+            const int sj = e / P, p = e - sj * P;
+            const double x = r.hrows ? r.hrows[e] : r.th[(size_t)sj * r.C * r.P + cbase + p];
+            if (x < r.pp_bounds[2 * p] || x > r.pp_bounds[2 * p + 1] || !(cq[2 * p + 1] > 0.0)) {
+                bad = true;
+            } else if (fp32) {
+                const float z = (float)(x - v[p]) * (float)cq[2 * p + 1];
+                facc += fmaf(-0.5f * z, z, (float)cq[2 * p]);
+            } else {
+                const double z = (x - v[p]) * cq[2 * p + 1];
+                acc += -0.5 * z * z + cq[2 * p];
             }
         }
-        acc += (double)ks - (double)kc;
+        acc += (double)facc;
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        const bool oos = __any_sync(0xffffffffu, out_of_support);
-        if (lane == 0) out[q] = oos ? -INFINITY : acc;
+        bad = __any_sync(0xffffffffu, bad);
+        if (lane == 0) {
+            part[q * 32 + wid] = acc;
+            if (bad) oos[q] = 1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < m) {
+        const int q = threadIdx.x;
+        double sum = 0.0;
+        for (int w = 0; w < nw; ++w) sum += part[q * 32 + w];
+        out[q] = oos[q] ? -INFINITY : sum;
     }
     __syncthreads();
 }
@@ -1277,6 +1285,8 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
     __shared__ const double *s_vecs[kPhiBatch];
     __shared__ int s_chains[kPhiBatch];
     __shared__ double s_out[kPhiBatch];
+    __shared__ double s_part[kPhiBatch * 32];
+    __shared__ int s_oos[kPhiBatch];
     __shared__ int s_misc[4];
     const int type = r.pptype[0];
     if (type == PASS_SKIP) return;
@@ -1385,7 +1395,7 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
                     s_chains[threadIdx.x] = k;
                 }
                 __syncthreads();
-                phi_batch_hyper(r, s_vecs, s_chains, mb, s_cst, s_out);
+                phi_batch_hyper(r, s_vecs, s_chains, mb, s_cst, s_part, s_oos, s_out);
                 for (int q = threadIdx.x; q < mb; q += blockDim.x) {
                     const int k = s_list[q0 + q];
                     if (s_lps[k] > -INFINITY) s_lls[k] = s_out[q];
@@ -1431,7 +1441,7 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
                     s_lps[0] = phi_prior(r, r.pth_s + (size_t)i * P);
                 }
                 __syncthreads();
-                phi_batch_hyper(r, s_vecs, s_chains, refresh ? 2 : 1, s_cst, s_out);
+                phi_batch_hyper(r, s_vecs, s_chains, refresh ? 2 : 1, s_cst, s_part, s_oos, s_out);
                 if (threadIdx.x == 0) {
                     r.plp_s[i] = s_lps[0];
                     r.pll_s[i] = (s_lps[0] > -INFINITY) ? s_out[0] : 0.0;
