@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -40,6 +41,36 @@ ggdmc_status fail(ggdmc_status s, const std::string &msg)
         if (e_ != cudaSuccess)                                                           \
             return fail(GGDMC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
+
+// Scratch for ggdmc_logprior_noalloc: one fixed array per device, so that
+// entry point never allocates.  It holds the prior rows, then theta, then the
+// output, each starting on a 256-byte boundary.
+constexpr size_t kScratchDoubles = (size_t)1 << 17;   // 1 MiB
+static __device__ __align__(256) double g_scratch[kScratchDoubles];
+
+constexpr size_t kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double *g_scratch_ptr[kMaxDevices];
+
+size_t round256(size_t n_double) { return (n_double + 31) & ~(size_t)31; }
+
+// Device address of g_scratch on the current device, looked up once per
+// device (the lookup may load the module, so make the first call outside any
+// stream capture).
+ggdmc_status scratch_base(double **out)
+{
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (dev < 0 || (size_t)dev >= kMaxDevices) return fail(GGDMC_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        CU(cudaGetSymbolAddress(&p, g_scratch));
+        g_scratch_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return GGDMC_OK;
+}
 
 template <class T>
 struct DevBuf {
@@ -950,6 +981,31 @@ ggdmc_status ggdmc_logprior(const ggdmc_prior *prior, const double *theta, int32
     cudaFree(d_th);
     cudaFree(d_out);
     if (e) return fail(GGDMC_ERR_CUDA, std::string("logprior: ") + cudaGetErrorString(e));
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_logprior_noalloc(const ggdmc_prior *prior, const double *theta, int32_t n, double *out)
+{
+    if (!theta || !out || n < 1) return fail(GGDMC_ERR_ARG, "bad logprior arguments");
+    std::vector<double> rows;
+    ggdmc_status s = prior_rows(prior, rows);
+    if (s) return s;
+    const int P = prior->n_par;
+    const size_t n_rows = rows.size(), n_th = (size_t)n * P;
+    const size_t need = round256(n_rows) + round256(n_th) + round256((size_t)n);
+    if (need > kScratchDoubles)
+        return fail(GGDMC_ERR_ARG, "logprior_noalloc: " + std::to_string(n) + " vectors of " +
+                                       std::to_string(P) + " parameters need " + std::to_string(need * 8) +
+                                       " bytes of scratch; the limit is " +
+                                       std::to_string(kScratchDoubles * 8) + " bytes");
+    double *base = nullptr;
+    s = scratch_base(&base);
+    if (s) return s;
+    double *d_rows = base, *d_th = d_rows + round256(n_rows), *d_out = d_th + round256(n_th);
+    CU(cudaMemcpy(d_rows, rows.data(), sizeof(double) * n_rows, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d_th, theta, sizeof(double) * n_th, cudaMemcpyHostToDevice));
+    CU(launch_logprior(d_rows, P, d_th, n, d_out, nullptr));
+    CU(cudaMemcpy(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost));
     return GGDMC_OK;
 }
 

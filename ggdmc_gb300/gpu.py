@@ -51,6 +51,8 @@ def lib():
     L.ggdmc_trial_logdens.argtypes = [C.c_void_p, P(C.c_double), C.c_int32, P(C.c_double)]
     L.ggdmc_logprior.restype = St
     L.ggdmc_logprior.argtypes = [P(abi.Prior), P(C.c_double), C.c_int32, P(C.c_double)]
+    L.ggdmc_logprior_noalloc.restype = St
+    L.ggdmc_logprior_noalloc.argtypes = [P(abi.Prior), P(C.c_double), C.c_int32, P(C.c_double)]
     L.ggdmc_loghlike.restype = St
     L.ggdmc_loghlike.argtypes = [P(abi.Prior), P(C.c_double), P(C.c_double), C.c_int32,
                                  C.c_int32, P(C.c_double)]
@@ -222,6 +224,16 @@ def logprior(p_table, theta):
     th = m.keep(np.ascontiguousarray(np.atleast_2d(theta), np.float64))
     out = np.zeros(th.shape[0])
     check(lib().ggdmc_logprior(C.byref(p), abi.dptr(th), th.shape[0], abi.dptr(out)))
+    return out
+
+
+def logprior_noalloc(p_table, theta):
+    """logprior through the entry point that stages in a fixed device array."""
+    m = abi.Marshal()
+    p = m.prior(p_table)
+    th = m.keep(np.ascontiguousarray(np.atleast_2d(theta), np.float64))
+    out = np.zeros(th.shape[0])
+    check(lib().ggdmc_logprior_noalloc(C.byref(p), abi.dptr(th), th.shape[0], abi.dptr(out)))
     return out
 
 

@@ -247,6 +247,17 @@ ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta,
 ggdmc_status ggdmc_logprior(const ggdmc_prior *prior, const double *theta,
                             int32_t n, double *out);
 
+/* sumlogprior as ggdmc_logprior, without allocating: no counterpart in the
+ * reference.  Stages the prior rows, theta and the output in a fixed 1 MiB
+ * device array (one per device) instead of cudaMalloc; nothing in it needs to
+ * start at zero.  Sizes whose staging (each piece rounded up to 256 bytes)
+ * exceeds 1 MiB return GGDMC_ERR_ARG before any device work.  Calls that
+ * overlap on one device (two host threads) share the array and race.  The
+ * first call on a device looks up the array's address, which may load the
+ * module: make it outside any stream capture. */
+ggdmc_status ggdmc_logprior_noalloc(const ggdmc_prior *prior, const double *theta,
+                                    int32_t n, double *out);
+
 /* sumloghlike (src/de.cpp:245-270): phi [n][2P], subject thetas
  * [n_subject][n][P] (chain j of every subject pairs with phi j) -> out [n]. */
 ggdmc_status ggdmc_loghlike(const ggdmc_prior *p_prior, const double *phi,
