@@ -7,6 +7,7 @@ A step is one DE sweep: the phi level and every subject, all chains
 it), batched mixed precision, exact reference chain order.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--no-cpu] [--profile]
 
 --impl reference times the reference's algorithm on the host cores: the
 CPU restatement in oracle/ (the reference itself needs R and packages that
@@ -213,6 +214,10 @@ def run_ours(args):
         wall = time.perf_counter() - t0
     st = out["stats"]
     ms = st["sweep_ms"]
+    if args.profile:
+        lk_ms, lk_evals = loglik_roofline(w, h, n_launch=2)
+        log(f"profile mode: {args.steps} sweeps in {ms:.3f} ms; likelihood launch {lk_ms:.3f} ms")
+        return
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -335,6 +340,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", action="store_true",
+                    help="warm-up and timed sweeps only (for ncu launch lists and captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

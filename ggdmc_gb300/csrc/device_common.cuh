@@ -45,7 +45,37 @@ __device__ __forceinline__ double uniform(const DrawSrc &d, int64_t it, int64_t 
 // -------------------------------------------------------------- normals
 __device__ __forceinline__ double Phi64(double z) { return 0.5 * erfc(-z * 0.70710678118654752440); }
 __device__ __forceinline__ double phi64(double z) { return exp(-0.5 * z * z) * 0.39894228040143267794; }
-__device__ __forceinline__ float phi32(float z) { return expf(-0.5f * z * z) * 0.398942280f; }
+// phi in FP32 with the square split exactly (z*z = h + l), so the exponent
+// keeps full relative accuracy for large |z|: exp(-h/2) (1 - l/2).
+__device__ __forceinline__ float phi32(float z)
+{
+    const float h = z * z, l = fmaf(z, z, -h);
+    const float e = expf(-0.5f * h) * 0.398942280f;
+    return fmaf(e, -0.5f * l, e);
+}
+
+// Mills ratio M(x) = Q(x)/phi(x), x >= 0: rational P4/Q5 fitted for minimax
+// relative error on [0, 14] (fit_mills.py; 5.5e-9 exact, 3.2e-7 in FP32).
+// Beyond 14, phi(x) underflows FP32, so the clamp does not change a product.
+__device__ __forceinline__ float mills32(float x)
+{
+    x = fminf(x, 14.f);
+    const float p = fmaf(fmaf(fmaf(fmaf(__int_as_float(0x3c2779df), x, __int_as_float(0x3dcf447b)), x,
+                                   __int_as_float(0x3eea2de0)), x, __int_as_float(0x3f8c4b52)), x,
+                         __int_as_float(0x3fa06c99));
+    const float q = fmaf(fmaf(fmaf(fmaf(fmaf(__int_as_float(0x3c277955), x, __int_as_float(0x3dcf480d)), x,
+                                        __int_as_float(0x3eef5540)), x, __int_as_float(0x3f99834b)), x,
+                              __int_as_float(0x3fd61160)), x, 1.f);
+    return __fdividef(p, q);
+}
+
+// Phi(x) from phx = phi(x): the lower tail phi(x) M(-x) for x < 0, else
+// 1 - phi(x) M(x).
+__device__ __forceinline__ float ncdf32(float x, float phx)
+{
+    const float t = phx * mills32(fabsf(x));
+    return (x < 0.f) ? t : 1.f - t;
+}
 
 // ------------------------------------------------------ FP64 LBA trial
 // The reference form (ggdmcLikelihood, restated): node-1 pdf floored at
@@ -103,7 +133,7 @@ __device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int 
         const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
         const float pz = phi32(cz), pm = phi32(czm);
         const float sg = (czm >= 0.f) ? -1.f : 1.f;
-        const float d = sg * (normcdff(sg * cz) - normcdff(sg * czm));
+        const float d = sg * (ncdf32(sg * cz, pz) - ncdf32(sg * czm, pm));
         pdf = fmaf(b.x, d, a.w * (pm - pz));
     }
     float surv = 1.f;
@@ -116,7 +146,7 @@ __device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int 
         const float pz = phi32(cz), pm = phi32(czm);
         const bool late = cz < 0.f;
         const float sg = late ? 1.f : -1.f;
-        const float br = fmaf(cz, normcdff(sg * cz), -czm * normcdff(sg * czm)) + sg * (pz - pm);
+        const float br = fmaf(cz, ncdf32(sg * cz, pz), -czm * ncdf32(sg * czm, pm)) + sg * (pz - pm);
         const float tcs = t * a.w;
         const float S = late ? fmaf(tcs, br, -b.y) : fmaf(-tcs, br, 1.f);
         surv *= S;

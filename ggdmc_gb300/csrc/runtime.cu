@@ -162,7 +162,7 @@ struct ggdmc_handle {
     DevBuf<double> th, lp, ll, th_s, lp_s, ll_s, phi_tab, pp_bounds, prior, hprior, hrows;
     DevBuf<double> pth, plp, pll, pth_s, plp_s, pll_s, pref_src, pref_next;
     DevBuf<int32_t> partner, ptype, nstep, sub, migrated, ppartner, pptype, pnstep, psub,
-        pmigrated, iter, status, items, items_plain, rs_para;
+        pmigrated, iter, status, items, items_plain, rs_para, sub_order;
     DevBuf<int8_t> need, pneed;
     DevBuf<float4> tab_a;
     DevBuf<float2> tab_b, tab_t;
@@ -481,6 +481,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         for (size_t q = 0; q < plain.size(); ++q) plain[q] = (int32_t)q;
         CU(h->items.upload(items.data(), items.size(), st));
         CU(h->items_plain.upload(plain.data(), plain.size(), st));
+        CU(h->sub_order.upload(order.data(), order.size(), st));
     }
     if (Pphi > 0) {
         CU(h->pth.alloc((size_t)C * Pphi));
@@ -552,6 +553,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.jit = h->jit.p; r.accu = h->accu.p;
     r.tab_a = h->tab_a.p; r.tab_b = h->tab_b.p; r.tab_t = h->tab_t.p; r.tab_bad = h->tab_bad.p;
     r.rs_para = h->rs_para.p; r.CS = CS;
+    r.sub_order = h->sub_order.p;
     r.pjit = h->pjit.p; r.paccu = h->paccu.p;
     r.prior = (!hier && !hyper) ? h->prior.p : nullptr;
     r.pp_bounds = (hier || hyper) ? h->pp_bounds.p : nullptr;

@@ -70,6 +70,7 @@ struct RunDev {
     double *jit;                   // [S][C][P] jitter draws of the pass (re-proposals reuse them)
     double *accu;                  // [S][C]    Metropolis accept uniforms of the pass
     int32_t *rs_para;              // [S] blocked parameter of the pass, -1 for all
+    const int32_t *sub_order;      // [S] subjects by trial count, largest first
     int32_t CS;                    // proposal slots per level: C speculative + C variants
     // FP32 tables of every proposal slot, built where the proposal is built
     float4 *tab_a;                 // [S*CS][n_ent] (b/s, (b-A)/s, v/s, s/(A Phi(v/s)))

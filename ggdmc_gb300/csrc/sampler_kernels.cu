@@ -22,14 +22,22 @@
 #include <cstdio>
 #include <cstdint>
 
+#include <cooperative_groups.h>
+
 #include "sampler.cuh"
 
 namespace ggdmc {
 
 constexpr int kLikThreads = 128;
 constexpr int kResolveThreads = 384;
+#ifndef GGDMC_RESOLVE_CLUSTER
+#define GGDMC_RESOLVE_CLUSTER 1
+#endif
+constexpr int kResolveCluster = GGDMC_RESOLVE_CLUSTER;   // CTAs per subject in resolve
+constexpr int kMigRound = 8;              // migration variants evaluated per resolve round
 constexpr int kPhiThreads = 256;
 constexpr int kProposeThreads = 128;
+constexpr int kPhiProposeThreads = 1024;   // one CTA: a warp per phi chain's prior
 
 // ------------------------------------------------------------- helpers
 __device__ __forceinline__ double block_sum(double v, double *red)
@@ -166,6 +174,15 @@ __device__ __forceinline__ double phi_prior(const RunDev &r, const double *th)
     double s = 0.0;
     for (int j = 0; j < r.Pphi; ++j) s += prior_term(r.hprior + kPriorRow * j, th[j]);
     return s;
+}
+
+// phi_prior with the warp's lanes over the parameters; every lane gets the sum.
+__device__ __forceinline__ double warp_phi_prior(const RunDev &r, const double *th)
+{
+    double s = 0.0;
+    for (int j = threadIdx.x & 31; j < r.Pphi; j += 32) s += prior_term(r.hprior + kPriorRow * j, th[j]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    return __shfl_sync(0xffffffffu, s, 0);
 }
 
 // Metropolis test of update_theta (src/de.cpp:81-108): accept iff
@@ -731,14 +748,50 @@ __global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int3
     eval_slots(r, l, s_slots, s_m, sm, r.prec == PREC_MIXED, nullptr);
 }
 
-// Ordered decisions of one subject level per CTA (src/de.cpp:111-199,
-// 567-665).  Decisions are taken from the speculative results while the
-// proposal a step would get in sequence is the one evaluated; a
-// crossover chain whose partner moved earlier in the sweep is re-proposed
-// from the current state and re-evaluated with the other stale chains of
-// its round.  Migration steps: each round evaluates the next kVariants steps
-// as if the steps before them accept (a cascade carries one value forward);
-// after a rejection the next step's start-of-pass proposal is valid again.
+// Barrier of the resolve cluster (a block barrier when it has one CTA); it
+// orders shared and global memory across the cluster's CTAs.
+__device__ __forceinline__ void cluster_barrier()
+{
+    if constexpr (kResolveCluster == 1) __syncthreads();
+    else cooperative_groups::this_cluster().sync();
+}
+
+// eval_slots across a cluster: each CTA sums its slice of the subject's
+// trials, the partials are exchanged through distributed shared memory and
+// every CTA adds them in rank order, so all CTAs hold identical totals.
+// out[slots[q] - out_off] = total of slot q; the lead CTA also stores ll_s.
+__device__ void eval_slots_cluster(const RunDev &r, int l, const int *slots, int m, SubSmem &sm, bool mixed,
+                                   double *part, double *out, int out_off, bool lead)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int Q = kResolveCluster, rank = (int)cl.block_rank();
+    const int N = (int)(r.offs[l + 1] - r.offs[l]);
+    const int i0 = (int)((int64_t)N * rank / Q), i1 = (int)((int64_t)N * (rank + 1) / Q);
+    for (int g0 = 0; g0 < m; g0 += kGroup) {
+        const int ng = min(kGroup, m - g0);
+        for (int g = 0; g < ng; ++g) load_slot(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
+        __syncthreads();
+        double o[kGroup];
+        group_loglik(r, l, i0, i1, sm, ng, mixed, o);
+        if (threadIdx.x == 0) {
+            for (int g = 0; g < ng; ++g) part[g0 + g] = o[g];
+            atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)(i1 - i0) * ng);
+        }
+        __syncthreads();
+    }
+    cluster_barrier();
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        double t = 0.0;
+        if constexpr (kResolveCluster == 1) t = part[q];
+        else
+            for (int k = 0; k < Q; ++k) t += cl.map_shared_rank(part, k)[q];
+        out[slots[q] - out_off] = t;
+        if (lead) r.ll_s[(size_t)l * r.CS + slots[q]] = t;
+    }
+    cluster_barrier();   // partials are read before any CTA overwrites them
+}
+
 struct ResSmem {
     double *lp, *ll;        // [C] current state
     double *lps, *lls;      // [C] proposal values of each step
@@ -751,12 +804,16 @@ struct ResSmem {
     int16_t *ver;           // [C]
     uint8_t *mod, *flag, *dec;   // [C]
     int *misc;              // 8
+    double *part;           // [C + kVariants] this CTA's partial sums of one evaluation
+    int *vr, *vs;           // [kVariants] migration variant w: last rejected step (-1: none
+                            // since the round began) and the step it serves
 };
 
 __host__ __device__ inline size_t res_smem_bytes(int C)
 {
     return align_up((size_t)C * (8 * sizeof(double) + 5 * sizeof(int) + sizeof(int16_t) + 3) +
-                        kVariants * sizeof(int) + 8 * sizeof(int) + 64, 16);
+                        kVariants * sizeof(int) + 8 * sizeof(int) + 64, 16) +
+           (size_t)(C + kVariants) * sizeof(double) + 2 * kVariants * sizeof(int);
 }
 
 __device__ ResSmem carve_res(char *base, int C)
@@ -780,15 +837,19 @@ __device__ ResSmem carve_res(char *base, int C)
     s.mod = (uint8_t *)(s.ver + C);
     s.flag = s.mod + C;
     s.dec = s.flag + C;
+    s.part = (double *)(base + align_up((size_t)C * (8 * sizeof(double) + 5 * sizeof(int) + sizeof(int16_t) + 3) +
+                                            kVariants * sizeof(int) + 8 * sizeof(int) + 64, 16));
+    s.vr = (int *)(s.part + C + kVariants);
+    s.vs = s.vr + kVariants;
     return s;
 }
 
 // Copy the rows of the steps accepted by the last scan into the state.
-__device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na)
+__device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na, bool lead)
 {
     const int C = r.C, P = r.P;
     const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
-    for (int q = threadIdx.x; q < na * P; q += blockDim.x) {
+    for (int q = threadIdx.x; lead && q < na * P; q += blockDim.x) {
         const int a = q / P, j = q % P;
         const int i = rs.acc[a];
         const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? rs.pa[0] : rs.pa[i + 1]);
@@ -800,24 +861,46 @@ __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &
         const int sl = rs.accslot[a];
         const double lpv = (sl < C) ? rs.lps[sl] : rs.vlp[sl - C];
         const double llv = (sl < C) ? rs.lls[sl] : rs.vll[sl - C];
-        r.lp[lc + dst] = lpv;
-        r.ll[lc + dst] = llv;
+        if (lead) {
+            r.lp[lc + dst] = lpv;
+            r.ll[lc + dst] = llv;
+        }
         rs.lp[dst] = lpv;
         rs.ll[dst] = llv;
     }
-    if (threadIdx.x == 0 && na) atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)na);
+    if (lead && threadIdx.x == 0 && na) atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)na);
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, int pass, int level_begin)
+// k_sub_resolve: ordered decisions of one subject level per cluster
+// (src/de.cpp:111-199, 567-665).  Decisions are taken from the speculative
+// results while the proposal a step would get in sequence is the one
+// evaluated; a crossover chain whose partner moved earlier in the sweep is
+// re-proposed from the current state and re-evaluated with the other stale
+// chains of its round.  Migration steps: the first round uses the start-of-
+// pass proposals (valid after a rejection) and the cascade from step 0 (valid
+// while every step accepts); later rounds evaluate the most likely values
+// the next steps can need.  With a cluster of several CTAs each CTA takes
+// the same decisions and evaluates a slice of the trials; the lead CTA alone
+// writes the chain state.
+#if GGDMC_RESOLVE_CLUSTER > 1
+#define GGDMC_RESOLVE_CLUSTER_DIMS __cluster_dims__(GGDMC_RESOLVE_CLUSTER, 1, 1)
+#else
+#define GGDMC_RESOLVE_CLUSTER_DIMS
+#endif
+__global__ void GGDMC_RESOLVE_CLUSTER_DIMS __launch_bounds__(kResolveThreads, 2)
+k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
 {
+    const int rank = (kResolveCluster == 1) ? 0 : (int)cooperative_groups::this_cluster().block_rank();
+    const bool lead = rank == 0;
+    const int slot_in_grid = blockIdx.x / kResolveCluster;
+    const int l = level_begin + (order ? order[slot_in_grid] : slot_in_grid);
     extern __shared__ __align__(16) char smem_raw[];
-    const int l = level_begin + blockIdx.x;
     const int type = r.ptype[l];
-    if (type == PASS_SKIP) return;
+    if (type == PASS_SKIP) return;   // uniform across the cluster
     const int n = r.nstep[l];
-    const int C = r.C, P = r.P, CS = r.CS;
-    const size_t lc = (size_t)l * C, ls = (size_t)l * CS;
+    const int C = r.C, P = r.P;
+    const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
     const bool mixed = r.prec == PREC_MIXED;
     SubSmem sm = carve(smem_raw, r.m);
     ResSmem rs = carve_res(smem_raw + sub_smem_bytes(r.m), C);
@@ -843,6 +926,8 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
     const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
     const int para = r.rs_para[l];
     const double *jit = r.jit + lc * P;
+    // work split of the re-proposals across the cluster
+    const int ct = rank * blockDim.x + threadIdx.x, cstride = kResolveCluster * blockDim.x;
     int rounds = 0, reevals = 0, variants = 0;
     int decided = 0;
 #ifdef GGDMC_PHASE_PROFILE
@@ -876,7 +961,7 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
             }
             __syncthreads();
             const int d = rs.misc[0];
-            write_accepts(r, l, type, n, rs, rs.misc[1]);
+            write_accepts(r, l, type, n, rs, rs.misc[1], lead);
             decided = d;
             PH_ADD(c_dec);
             if (decided >= n) break;
@@ -892,10 +977,10 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
                 }
                 rs.misc[2] = m;
             }
-            __syncthreads();
+            cluster_barrier();   // the lead's accepted states are visible to the cluster
             const int m = rs.misc[2];
             reevals += m;
-            for (int q = threadIdx.x; q < m * P; q += blockDim.x) {
+            for (int q = ct; q < m * P; q += cstride) {
                 const int k = rs.list[q / P], j = q % P;
                 const double tk = r.th[(lc + k) * P + j];
                 r.th_s[(ls + k) * P + j] =
@@ -904,8 +989,8 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
                                      jit[(size_t)k * P + j])
                         : tk;
             }
-            for (int q = threadIdx.x; q < m; q += blockDim.x) r.tab_bad[ls + rs.list[q]] = 0;
-            __syncthreads();
+            for (int q = ct; q < m; q += cstride) r.tab_bad[ls + rs.list[q]] = 0;
+            cluster_barrier();   // re-proposals visible
             const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
             for (int q = wid; q < m; q += nw) {
                 const int k = rs.list[q];
@@ -913,13 +998,15 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
                 if ((threadIdx.x & 31) == 0) {
                     rs.lps[k] = lp;
                     rs.lls[k] = 0.0;
-                    r.lp_s[ls + k] = lp;
-                    r.ll_s[ls + k] = 0.0;
+                    if (lead) {
+                        r.lp_s[ls + k] = lp;
+                        r.ll_s[ls + k] = 0.0;
+                    }
                 }
             }
             if (mixed) {
                 const int NU = r.m.n_ent + r.m.n_t0;
-                for (int q = threadIdx.x; q < m * NU; q += blockDim.x) {
+                for (int q = ct; q < m * NU; q += cstride) {
                     const int k = rs.list[q / NU];
                     store_entry(r, ls + k, r.th_s + (ls + k) * P, q % NU);
                 }
@@ -932,10 +1019,10 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
                     if (rs.lps[rs.list[q]] > -INFINITY) rs.list[e++] = rs.list[q];
                 rs.misc[3] = e;
             }
-            __syncthreads();
+            cluster_barrier();   // tables visible
             PH_ADD(c_rep);
             PH_T0();
-            eval_slots(r, l, rs.list, rs.misc[3], sm, mixed, rs.lls);
+            eval_slots_cluster(r, l, rs.list, rs.misc[3], sm, mixed, rs.part, rs.lls, 0, lead);
             PH_ADD(c_ev);
         }
     } else {
@@ -955,76 +1042,110 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
             ++rounds;
             PH_T0();
             const int d = decided;
-            const int nv = (d == 0) ? n : min(kVariants, n - d);
-            const bool spec0 = (d == 0) || !rs.mod[d - 1];   // step d's source is unchanged
+            // Round d > 0 starts because step d-1 was accepted, so step d's
+            // source moved.  The value step s needs is fixed by the last
+            // rejected step r before it: the spec proposal of step r+1 plus
+            // the jitters of steps r+2..s, or, with no reject since d, the
+            // new source plus the jitters of d..s.  Evaluate the kMigRound
+            // most likely of these, scored with this pass's acceptance so far.
             if (d > 0) {
-            // variants: V_d = theta_src(d) + jit_d, V_s = V_(s-1) + jit_s
-            for (int j = threadIdx.x; j < P; j += blockDim.x) {
-                double v = r.th[(lc + rs.pa[d]) * P + j];
-                for (int w = 0; w < nv; ++w) {
-                    if (updated(j, para, nloop)) v = __dadd_rn(v, jit[(size_t)(d + w) * P + j]);
+                if (threadIdx.x == 0) {
+                    int acc = 0;
+                    for (int k = 0; k < d; ++k) acc += rs.mod[k];
+                    const double a = (acc + 1.0) / (d + 2.0);
+                    double best[kMigRound] = {};
+                    int nv = 0;
+                    auto offer = [&](double sc, int vr, int vs) {
+                        int pos = nv;
+                        while (pos > 0 && best[pos - 1] < sc) --pos;
+                        if (pos >= kMigRound) return;
+                        const int last = (nv < kMigRound) ? nv : kMigRound - 1;
+                        for (int q = last; q > pos; --q) {
+                            best[q] = best[q - 1];
+                            rs.vr[q] = rs.vr[q - 1];
+                            rs.vs[q] = rs.vs[q - 1];
+                        }
+                        best[pos] = sc;
+                        rs.vr[pos] = vr;
+                        rs.vs[pos] = vs;
+                        if (nv < kMigRound) ++nv;
+                    };
+                    double ak = 1.0;
+                    for (int k = 0; k < kVariants && d + k < n; ++k, ak *= a)
+                        offer(k == 0 ? 2.0 : ak, -1, d + k);
+                    double reach = 1.0;
+                    for (int rj = d; rj < d + kVariants && rj < n; ++rj, reach *= 0.95) {
+                        double sc = (1.0 - a) * reach;
+                        for (int k = 1; k <= 3 && rj + 1 + k < n; ++k) {
+                            sc *= a;
+                            offer(sc, rj, rj + 1 + k);
+                        }
+                    }
+                    rs.misc[4] = nv;
+                }
+                __syncthreads();
+                const int nv = rs.misc[4];
+                for (int q = ct; q < nv * P; q += cstride) {
+                    const int w = q / P, j = q % P;
+                    const int vr = rs.vr[w], vs = rs.vs[w];
+                    double v = (vr < 0) ? r.th[(lc + rs.pa[d]) * P + j] : r.th_s[(ls + vr + 1) * P + j];
+                    if (updated(j, para, nloop))
+                        for (int t = (vr < 0) ? d : vr + 2; t <= vs; ++t) v = __dadd_rn(v, jit[(size_t)t * P + j]);
                     r.th_s[(ls + C + w) * P + j] = v;
                 }
-            }
-            for (int w = threadIdx.x; w < nv; w += blockDim.x) r.tab_bad[ls + C + w] = 0;
-            __syncthreads();
-            const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-            for (int w = wid; w < nv; w += nw) {
-                const double lp = warp_prior(r, r.th_s + (ls + C + w) * P, rs.pa[d + w]);
-                if ((threadIdx.x & 31) == 0) {
-                    rs.vlp[w] = lp;
-                    rs.vll[w] = 0.0;
+                for (int w = ct; w < nv; w += cstride) r.tab_bad[ls + C + w] = 0;
+                cluster_barrier();   // variants visible
+                const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+                for (int w = wid; w < nv; w += nw) {
+                    const double lp = warp_prior(r, r.th_s + (ls + C + w) * P, rs.pa[rs.vs[w]]);
+                    if ((threadIdx.x & 31) == 0) {
+                        rs.vlp[w] = lp;
+                        rs.vll[w] = 0.0;
+                    }
                 }
-            }
-            if (mixed) {
-                const int NU = r.m.n_ent + r.m.n_t0;
-                for (int q = threadIdx.x; q < nv * NU; q += blockDim.x) {
-                    const int w = q / NU;
-                    store_entry(r, ls + C + w, r.th_s + (ls + C + w) * P, q % NU);
+                if (mixed) {
+                    const int NU = r.m.n_ent + r.m.n_t0;
+                    for (int q = ct; q < nv * NU; q += cstride) {
+                        const int w = q / NU;
+                        store_entry(r, ls + C + w, r.th_s + (ls + C + w) * P, q % NU);
+                    }
                 }
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                int e = 0;
-                for (int w = spec0 ? 1 : 0; w < nv; ++w)
-                    if (rs.vlp[w] > -INFINITY) rs.list[e++] = C + w;
-                rs.misc[3] = e;
-            }
-            __syncthreads();
-            const int ne = rs.misc[3];
-            variants += ne;
-            PH_ADD(c_rep);
-            PH_T0();
-            if (ne) {
-                eval_slots(r, l, rs.list, ne, sm, mixed, nullptr);
-                for (int q = threadIdx.x; q < ne; q += blockDim.x)
-                    rs.vll[rs.list[q] - C] = r.ll_s[ls + rs.list[q]];
                 __syncthreads();
-            }
+                if (threadIdx.x == 0) {
+                    int e = 0;
+                    for (int w = 0; w < nv; ++w)
+                        if (rs.vlp[w] > -INFINITY) rs.list[e++] = C + w;
+                    rs.misc[3] = e;
+                }
+                cluster_barrier();   // tables visible
+                const int ne = rs.misc[3];
+                variants += ne;
+                PH_ADD(c_rep);
+                PH_T0();
+                if (ne) eval_slots_cluster(r, l, rs.list, ne, sm, mixed, rs.part, rs.vll, C, lead);
             }
             PH_ADD(c_ev);
             PH_T0();
             if (threadIdx.x == 0) {
-                int s = d, na = 0;
-                bool run = true;
+                const int nv = (d == 0) ? n : rs.misc[4];
+                int s = d, na = 0, lastrej = -1;
                 while (s < n) {
-                    int slot;
-                    double lpv, llv;
-                    if (s == d) {
-                        slot = spec0 ? s : C;
-                    } else if (run && s < d + nv) {
-                        slot = C + (s - d);
-                    } else if (!rs.mod[s - 1]) {
-                        slot = s;
+                    int slot = -1;
+                    if (s > 0 && !rs.mod[s - 1]) {
+                        slot = s;                    // source unchanged: the spec proposal
+                    } else if (d == 0) {
+                        slot = (s == 0) ? 0 : (lastrej < 0 ? C + s : -1);   // cascade from step 0
                     } else {
-                        break;
+                        for (int w = 0; w < nv; ++w)
+                            if (rs.vs[w] == s && rs.vr[w] == lastrej) slot = C + w;
                     }
-                    lpv = (slot < C) ? rs.lps[slot] : rs.vlp[slot - C];
-                    llv = (slot < C) ? rs.lls[slot] : rs.vll[slot - C];
+                    if (slot < 0) break;
+                    const double lpv = (slot < C) ? rs.lps[slot] : rs.vlp[slot - C];
+                    const double llv = (slot < C) ? rs.lls[slot] : rs.vll[slot - C];
                     const bool ok = mh_accept((lpv + llv) - rs.cur[s], rs.accu[s]);
                     rs.mod[s] = ok ? 1 : 0;
                     if (ok) { rs.acc[na] = s; rs.accslot[na] = slot; ++na; }
-                    else run = false;
+                    else lastrej = s;
                     ++s;
                 }
                 rs.misc[0] = s;
@@ -1032,17 +1153,18 @@ __global__ void __launch_bounds__(kResolveThreads, 2) k_sub_resolve(RunDev r, in
             }
             __syncthreads();
             decided = rs.misc[0];
-            write_accepts(r, l, type, n, rs, rs.misc[1]);
+            write_accepts(r, l, type, n, rs, rs.misc[1], lead);
+            if (decided < n) cluster_barrier();   // the lead's accepted states are visible
             PH_ADD(c_dec);
         }
     }
 #ifdef GGDMC_PHASE_PROFILE
-    if (threadIdx.x == 0 && *r.iter == 3)
+    if (lead && threadIdx.x == 0 && *r.iter == 3)
         printf("PHASE l=%d type=%d N=%d n=%d reevals=%d variants=%d rounds=%d dec=%lld rep=%lld ev=%lld tot=%lld\n",
                l, type, (int)(r.offs[l + 1] - r.offs[l]), n, reevals, variants, rounds, c_dec, c_rep, c_ev,
                clock64() - t_start);
 #endif
-    if (threadIdx.x == 0) {
+    if (lead && threadIdx.x == 0) {
         atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
         atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
         atomicAdd(&r.stats[ST_VARIANTS], (unsigned long long)variants);
@@ -1085,7 +1207,7 @@ __device__ double hyper_sum(const RunDev &r, const double *phv, int chain, doubl
     return block_sum(acc + (double)accf, red);
 }
 
-__global__ void __launch_bounds__(kPhiThreads) k_phi_propose(RunDev r, int pass)
+__global__ void __launch_bounds__(kPhiProposeThreads) k_phi_propose(RunDev r, int pass)
 {
     __shared__ double s_u[kMaxChain + 2];
     __shared__ int s_sub[kMaxChain];
@@ -1162,11 +1284,13 @@ __global__ void __launch_bounds__(kPhiThreads) k_phi_propose(RunDev r, int pass)
         r.pth_s[(size_t)k * P + j] = out;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double lp = phi_prior(r, r.pth_s + (size_t)k * P);
-        r.plp_s[k] = lp;
-        r.pll_s[k] = 0.0;
-        r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
+    for (int k = threadIdx.x >> 5; k < n; k += blockDim.x >> 5) {
+        const double lp = warp_phi_prior(r, r.pth_s + (size_t)k * P);
+        if ((threadIdx.x & 31) == 0) {
+            r.plp_s[k] = lp;
+            r.pll_s[k] = 0.0;
+            r.pneed[k] = (lp > -INFINITY) ? 1 : 0;
+        }
     }
 }
 
@@ -1238,17 +1362,35 @@ __device__ void phi_batch_hyper(const RunDev &r, const double *const *vecs, cons
         bool bad = false;
         double acc = 0.0;
         float facc = 0.f;
-        for (int e = threadIdx.x; e < nterm; e += blockDim.x) {
-            const int sj = e / P, p = e - sj * P;
-            const double x = r.hrows ? r.hrows[e] : r.th[(size_t)sj * r.C * r.P + cbase + p];
-            if (x < r.pp_bounds[2 * p] || x > r.pp_bounds[2 * p + 1] || !(cq[2 * p + 1] > 0.0)) {
-                bad = true;
-            } else if (fp32) {
-                const float z = (float)(x - v[p]) * (float)cq[2 * p + 1];
-                facc += fmaf(-0.5f * z, z, (float)cq[2 * p]);
-            } else {
-                const double z = (x - v[p]) * cq[2 * p + 1];
-                acc += -0.5 * z * z + cq[2 * p];
+        // loads first, eight per thread in flight, then branch-free terms
+        constexpr int U = 8;
+        for (int e0 = threadIdx.x; e0 < nterm; e0 += U * blockDim.x) {
+            double x[U];
+            int pp[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + u * blockDim.x;
+                pp[u] = -1;
+                x[u] = 0.0;
+                if (e < nterm) {
+                    const int sj = e / P;
+                    pp[u] = e - sj * P;
+                    x[u] = r.hrows ? r.hrows[e] : r.th[(size_t)sj * r.C * r.P + cbase + pp[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int p = pp[u];
+                if (p < 0) continue;
+                const double xv = x[u];
+                bad |= (xv < r.pp_bounds[2 * p]) | (xv > r.pp_bounds[2 * p + 1]) | !(cq[2 * p + 1] > 0.0);
+                if (fp32) {
+                    const float z = (float)(xv - v[p]) * (float)cq[2 * p + 1];
+                    facc += fmaf(-0.5f * z, z, (float)cq[2 * p]);
+                } else {
+                    const double z = (xv - v[p]) * cq[2 * p + 1];
+                    acc += -0.5 * z * z + cq[2 * p];
+                }
             }
         }
         acc += (double)facc;
@@ -1377,10 +1519,13 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
                         : tk;
             }
             __syncthreads();
-            for (int q = threadIdx.x; q < m; q += blockDim.x) {
+            for (int q = threadIdx.x >> 5; q < m; q += blockDim.x >> 5) {
                 const int k = s_list[q];
-                s_lps[k] = phi_prior(r, r.pth_s + (size_t)k * P);
-                s_lls[k] = 0.0;
+                const double lp = warp_phi_prior(r, r.pth_s + (size_t)k * P);
+                if ((threadIdx.x & 31) == 0) {
+                    s_lps[k] = lp;
+                    s_lls[k] = 0.0;
+                }
             }
             __syncthreads();
 #ifdef GGDMC_PHASE_PROFILE
@@ -1433,12 +1578,15 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
                         ? __dadd_rn(r.pth[(size_t)src * P + j], r.pjit[(size_t)i * P + j])
                         : r.pth[(size_t)src * P + j];
                 __syncthreads();
-                if (threadIdx.x == 0) {
-                    s_vecs[0] = r.pth_s + (size_t)i * P;
-                    s_vecs[1] = r.pth + (size_t)src * P;
-                    s_chains[0] = src;
-                    s_chains[1] = src;
-                    s_lps[0] = phi_prior(r, r.pth_s + (size_t)i * P);
+                if (threadIdx.x < 32) {
+                    const double lp = warp_phi_prior(r, r.pth_s + (size_t)i * P);
+                    if (threadIdx.x == 0) {
+                        s_vecs[0] = r.pth_s + (size_t)i * P;
+                        s_vecs[1] = r.pth + (size_t)src * P;
+                        s_chains[0] = src;
+                        s_chains[1] = src;
+                        s_lps[0] = lp;
+                    }
                 }
                 __syncthreads();
                 phi_batch_hyper(r, s_vecs, s_chains, refresh ? 2 : 1, s_cst, s_part, s_oos, s_out);
@@ -1636,8 +1784,10 @@ cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
                                cudaStream_t st)
 {
-    k_sub_resolve<<<level_count, kResolveThreads, sub_smem_bytes(r.m) + res_smem_bytes(r.C), st>>>(
-        r, pass, level_begin);
+    // every subject at once runs largest first; a single subject keeps its index
+    const int32_t *order = (level_count == r.S) ? r.sub_order : nullptr;
+    k_sub_resolve<<<level_count * kResolveCluster, kResolveThreads,
+                    sub_smem_bytes(r.m) + res_smem_bytes(r.C), st>>>(r, pass, level_begin, order);
     return cudaGetLastError();
 }
 
@@ -1649,7 +1799,7 @@ cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st)
 
 cudaError_t launch_phi_propose(const RunDev &r, int pass, cudaStream_t st)
 {
-    k_phi_propose<<<1, kPhiThreads, 0, st>>>(r, pass);
+    k_phi_propose<<<1, kPhiProposeThreads, 0, st>>>(r, pass);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,23 @@ def test_mixed_loglik_uneven_256(oracle, spread):
     assert np.all(err <= 1e-6), err.max()
 
 
+def test_mixed_trial_logdens_per_trial(oracle):
+    # each FP32 trial density against the FP64 oracle: within 5e-5 absolute
+    # (the late-survivor form may amplify FP32 rounding up to 32x before the
+    # FP64 fallback takes over) and typically within 1e-6
+    w = synth.uneven_lba_256(n_subject=48)
+    rng = np.random.default_rng(4)
+    theta = near_truth(w, 1, rng, 0.05)[:, 0, :]
+    h = gpu.Handle(w.model, w.batch)
+    got = h.trial_logdens(theta, abi.MIXED)
+    want = np.concatenate([
+        oracle.sumloglike(w.model, w.batch.subject(s).rt, w.batch.subject(s).cell, theta[s],
+                          per_trial=True)[1] for s in range(w.batch.n_subject)])
+    err = np.abs(got - want)
+    assert err.max() <= 5e-5, err.max()
+    assert np.median(err) <= 1e-6, np.median(err)
+
+
 def test_mixed_loglik_fixtures_close(oracle):
     # prior draws of the fixtures: wild parameters, many FP64 re-evaluations
     z, model, _, pop = load_fixture(6)
