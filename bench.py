@@ -34,6 +34,8 @@ sys.path.insert(0, ROOT)
 from ggdmc_gb300 import abi, synth  # noqa: E402
 
 WORKLOAD = "uneven_lba_256"
+E2E_MAX_STEPS = 50                       # samples of every chain come back: 2.1 MB per sweep
+PROFILE = os.path.join(ROOT, "profiles", "k_loglik_batch_uneven_lba_256.md")
 K_ACC = 4
 FLOPS_PER_EVAL = 17 * K_ACC + 2          # algorithmic flops of one LBA trial density
 TRANS_PER_EVAL = 4 * K_ACC + 1           # Phi / phi / log evaluations
@@ -62,7 +64,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -122,6 +124,27 @@ def cfg_for(w, steps, precision, flags=0, seed=2025):
     return abi.DEConfigPy(nchain=w.nchain, nparameter=2 * w.model.n_par, nmc=steps + 1, thin=1,
                           pop_migration_prob=0.05, sub_migration_prob=0.06, precision=precision,
                           seed=seed, flags=flags)
+
+
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the likelihood kernel from the committed ncu
+    summary (dram__bytes_read.sum + dram__bytes_write.sum), or None."""
+    try:
+        with open(PROFILE) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1].strip())
+    except OSError:
+        pass
+    return None
 
 
 def loglik_roofline(w, h, n_launch=10):
@@ -238,17 +261,24 @@ def run_ours(args):
     lk_ms, lk_evals = loglik_roofline(w, h)
     ach_tflops = lk_evals * FLOPS_PER_EVAL / (lk_ms * 1e-3) / 1e12
     ach_mufu = lk_evals * TRANS_PER_EVAL / (lk_ms * 1e-3) / 1e12
+    # its algorithmic bytes: each trial (float2 time + uint16 cell) once, the
+    # theta vectors and the per-(subject, proposal) sums
+    S_, C_, P_ = w.batch.n_subject, w.nchain, w.model.n_par
+    lk_bytes = len(w.batch.rt) * 10 + S_ * C_ * P_ * 8 + S_ * C_ * 8
+    hbm_peak = measured_hbm_gbs()
 
-    # end to end through the one-shot C ABI with host buffers
+    # end to end through the one-shot C ABI with host buffers: upload of the
+    # trials and chain states, the sweeps, download of every sample
+    e2e_steps = min(args.steps, E2E_MAX_STEPS)
     t0 = time.perf_counter()
-    e2e = gpu.run(cfg_for(w, args.steps, abi.MIXED), w.model, w.batch, w.p_prior, w.h_prior,
+    e2e = gpu.run(cfg_for(w, e2e_steps, abi.MIXED), w.model, w.batch, w.p_prior, w.h_prior,
                   phi, subj)
     e2e_s = time.perf_counter() - t0
     S, Cn, P = w.batch.n_subject, w.nchain, w.model.n_par
     h2d = (w.batch.rt.nbytes + w.batch.cell.nbytes + w.batch.offsets.nbytes
            + subj[0].nbytes + subj[1].nbytes + subj[2].nbytes
            + phi[0].nbytes + phi[1].nbytes + phi[2].nbytes)
-    d2h = 8 * (S * (args.steps + 1) * Cn * (P + 2) + (args.steps + 1) * Cn * (2 * P + 2)
+    d2h = 8 * (S * (e2e_steps + 1) * Cn * (P + 2) + (e2e_steps + 1) * Cn * (2 * P + 2)
                + S * Cn * (P + 2) + Cn * (2 * P + 2))
 
     line = {
@@ -278,15 +308,22 @@ def run_ours(args):
         "roofline": {"kernel": "loglik (k_loglik_batch = k_sub_loglik body)",
                      "bound": "fp32", "achieved": round(ach_tflops, 3),
                      "peak": round(peak_fp32, 3), "unit": "TFLOP/s",
-                     "frac": round(ach_tflops / peak_fp32, 4), "traffic": None,
+                     "frac": round(ach_tflops / peak_fp32, 4), "traffic": profiled_traffic(),
                      "flops_per_eval": FLOPS_PER_EVAL, "evals_per_launch": lk_evals,
                      "launch_ms": round(lk_ms, 4),
                      "peak_source": "measured (ggdmc_probe_peaks FMA loop)",
                      "sfu": {"achieved_tops": round(ach_mufu, 4), "peak_tops": round(peak_mufu, 4),
                              "frac": round(ach_mufu / peak_mufu, 4),
-                             "transcendentals_per_eval": TRANS_PER_EVAL}},
-        "e2e": {"value": round(args.steps / e2e_s, 3), "unit": "DE sweeps/s",
-                "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps),
+                             "transcendentals_per_eval": TRANS_PER_EVAL},
+                     "hbm_view": {"algorithmic_bytes": int(lk_bytes),
+                                  "achieved_gbs": round(lk_bytes / (lk_ms * 1e-3) / 1e9, 2),
+                                  "peak_gbs": hbm_peak,
+                                  "frac": (round(lk_bytes / (lk_ms * 1e-3) / 1e9 / hbm_peak, 5)
+                                           if hbm_peak else None),
+                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}},
+        "e2e": {"value": round(e2e_steps / e2e_s, 3), "unit": "DE sweeps/s",
+                "h2d_bytes_per_step": int(h2d // e2e_steps), "d2h_bytes_per_step": int(d2h // e2e_steps),
+                "steps": e2e_steps,
                 "call": "ggdmc_run (one-shot C ABI: upload, sweeps, sample download)"},
         "clocks": clk.summary(),
         "wall_s_timed_run": round(wall, 3),
@@ -336,7 +373,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")

@@ -36,7 +36,7 @@ constexpr int kResolveThreads = 384;
 constexpr int kResolveCluster = GGDMC_RESOLVE_CLUSTER;   // CTAs per subject in resolve
 constexpr int kMigRound = 8;              // migration variants evaluated per resolve round
 constexpr int kPhiThreads = 256;
-constexpr int kProposeThreads = 128;
+constexpr int kProposeThreads = 512;
 constexpr int kPhiProposeThreads = 1024;   // one CTA: a warp per phi chain's prior
 
 // ------------------------------------------------------------- helpers
@@ -695,12 +695,27 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
     const int nv = (type == PASS_MIG) ? n : 0;
     for (int w = nv + threadIdx.x; w < C; w += blockDim.x) r.need[(size_t)l * CS + C + w] = 0;
     if (nv) {
-        for (int j = threadIdx.x; j < P; j += blockDim.x) {
-            double v = th[(size_t)s_sub[0] * P + j];
-            for (int w = 0; w < nv; ++w) {
-                if (updated(j, para, nloop)) v = __dadd_rn(v, jit[(size_t)w * P + j]);
-                ths[(size_t)(C + w) * P + j] = v;
+        // the running sums in shared memory (s_u, whose draws are consumed),
+        // then one parallel store; jit was written above by this block
+        double *s_v = s_u;
+        constexpr int kCap = kMaxChain + 2;
+        for (int w0 = 0; w0 < nv; w0 += kCap / P) {
+            const int wn = min(nv - w0, kCap / P);
+            __syncthreads();
+            for (int q = threadIdx.x; q < wn * P; q += blockDim.x) s_v[q] = jit[(size_t)(w0 + q / P) * P + q % P];
+            __syncthreads();
+            for (int j = threadIdx.x; j < P; j += blockDim.x) {
+                double v = (w0 == 0) ? th[(size_t)s_sub[0] * P + j] : ths[(size_t)(C + w0 - 1) * P + j];
+                const bool up = updated(j, para, nloop);
+                for (int w = 0; w < wn; ++w) {
+                    if (up) v = __dadd_rn(v, s_v[w * P + j]);
+                    s_v[w * P + j] = v;
+                }
             }
+            __syncthreads();
+            for (int q = threadIdx.x; q < wn * P; q += blockDim.x)
+                ths[(size_t)(C + w0 + q / P) * P + q % P] = s_v[q];
+            __syncthreads();
         }
         for (int w = threadIdx.x; w < nv; w += blockDim.x) r.tab_bad[(size_t)l * CS + C + w] = 0;
         __syncthreads();
@@ -816,6 +831,14 @@ __host__ __device__ inline size_t res_smem_bytes(int C)
            (size_t)(C + kVariants) * sizeof(double) + 2 * kVariants * sizeof(int);
 }
 
+// The subject's jitter rows are staged in shared memory when they fit.
+constexpr size_t kJitStage = 32768;
+__host__ __device__ inline size_t jit_stage_bytes(int C, int P)
+{
+    const size_t b = (size_t)C * P * sizeof(double);
+    return b <= kJitStage ? b : 0;
+}
+
 __device__ ResSmem carve_res(char *base, int C)
 {
     ResSmem s;
@@ -926,6 +949,12 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
     const int nloop = (r.loop == LOOP_HCHAINS) ? r.half : r.Pn;
     const int para = r.rs_para[l];
     const double *jit = r.jit + lc * P;
+    if (jit_stage_bytes(C, P)) {
+        double *js = (double *)(smem_raw + sub_smem_bytes(r.m) + res_smem_bytes(C));
+        for (int q = threadIdx.x; q < C * P; q += blockDim.x) js[q] = jit[q];
+        __syncthreads();
+        jit = js;
+    }
     // work split of the re-proposals across the cluster
     const int ct = rank * blockDim.x + threadIdx.x, cstride = kResolveCluster * blockDim.x;
     int rounds = 0, reevals = 0, variants = 0;
@@ -1038,6 +1067,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
             rs.vll[w] = r.ll_s[ls + C + w];
         }
         __syncthreads();
+        int mig_acc = 0;   // accepted steps so far (thread 0's count)
         while (decided < n) {
             ++rounds;
             PH_T0();
@@ -1050,9 +1080,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
             // most likely of these, scored with this pass's acceptance so far.
             if (d > 0) {
                 if (threadIdx.x == 0) {
-                    int acc = 0;
-                    for (int k = 0; k < d; ++k) acc += rs.mod[k];
-                    const double a = (acc + 1.0) / (d + 2.0);
+                    const double a = (mig_acc + 1.0) / (d + 2.0);
                     double best[kMigRound] = {};
                     int nv = 0;
                     auto offer = [&](double sc, int vr, int vs) {
@@ -1144,7 +1172,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
                     const double llv = (slot < C) ? rs.lls[slot] : rs.vll[slot - C];
                     const bool ok = mh_accept((lpv + llv) - rs.cur[s], rs.accu[s]);
                     rs.mod[s] = ok ? 1 : 0;
-                    if (ok) { rs.acc[na] = s; rs.accslot[na] = slot; ++na; }
+                    if (ok) { rs.acc[na] = s; rs.accslot[na] = slot; ++na; ++mig_acc; }
                     else lastrej = s;
                     ++s;
                 }
@@ -1761,7 +1789,7 @@ cudaError_t configure_kernels(const DevModel &m)
     if ((e = cudaFuncSetAttribute(k_sub_loglik, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
     if ((e = cudaFuncSetAttribute(k_sub_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  bytes + (int)res_smem_bytes(kMaxChain))))
+                                  bytes + (int)res_smem_bytes(kMaxChain) + (int)kJitStage)))
         return e;
     if ((e = cudaFuncSetAttribute(k_loglik_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
@@ -1787,7 +1815,8 @@ cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int l
     // every subject at once runs largest first; a single subject keeps its index
     const int32_t *order = (level_count == r.S) ? r.sub_order : nullptr;
     k_sub_resolve<<<level_count * kResolveCluster, kResolveThreads,
-                    sub_smem_bytes(r.m) + res_smem_bytes(r.C), st>>>(r, pass, level_begin, order);
+                    sub_smem_bytes(r.m) + res_smem_bytes(r.C) + jit_stage_bytes(r.C, r.P), st>>>(
+        r, pass, level_begin, order);
     return cudaGetLastError();
 }
 
