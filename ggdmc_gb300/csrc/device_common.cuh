@@ -161,4 +161,141 @@ __device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int 
     return true;
 }
 
+// ------------------------------------------------------ DDM trial
+// Navarro & Fuss (2009) first-passage density of the Wiener process at the
+// lower boundary, with the series length chosen from its error bounds;
+// drift variability sv integrated in closed form, start-point (sz) and
+// non-decision-time (st0) variability by the midpoint rule on kDdmNz x kDdmNt
+// nodes.  The entry of a (cell, proposal) holds the responding boundary's
+// mirrored values: p[0] a, p[1] v (negated for the upper boundary), p[2] z/a
+// (1 - z/a for the upper), p[3] the response's non-decision time
+// (t0 - d/2 upper, t0 + d/2 lower), p[4] sz, p[5] sv, p[6] st0.
+constexpr int kDdmNz = 8, kDdmNt = 8;
+constexpr double kDdmEps = 1e-10;
+
+__device__ __forceinline__ double nf_density64(double tt, double w)
+{
+    if (!(tt > 0.0)) return 0.0;
+    const double pi = 3.14159265358979323846;
+    double ks, kl;
+    if (pi * tt * kDdmEps < 1.0) {
+        kl = sqrt(-2.0 * log(pi * tt * kDdmEps) / (pi * pi * tt));
+        const double lb = 1.0 / (pi * sqrt(tt));
+        if (kl < lb) kl = lb;
+    } else {
+        kl = 1.0 / (pi * sqrt(tt));
+    }
+    if (2.0 * sqrt(2.0 * pi * tt) * kDdmEps < 1.0) {
+        ks = 2.0 + sqrt(-2.0 * tt * log(2.0 * sqrt(2.0 * pi * tt) * kDdmEps));
+        const double lb = sqrt(tt) + 1.0;
+        if (ks < lb) ks = lb;
+    } else {
+        ks = 2.0;
+    }
+    double p = 0.0;
+    if (ks < kl) {
+        const int K = (int)ceil(ks);
+        for (int k = -((K - 1) / 2); k <= (K - 1) / 2; ++k) {
+            const double x = w + 2.0 * k;
+            p += x * exp(-(x * x) / (2.0 * tt));
+        }
+        p /= sqrt(2.0 * pi * tt * tt * tt);
+    } else {
+        const int K = (int)ceil(kl);
+        for (int k = 1; k <= K; ++k) p += k * exp(-(double)(k * k) * (pi * pi * tt / 2.0)) * sinpi(k * w);
+        p *= pi;
+    }
+    return p;
+}
+
+__device__ __forceinline__ double ddm_fixed64(double t, double a, double v, double w, double sv)
+{
+    if (!(t > 0.0)) return 0.0;
+    const double g = nf_density64(t / (a * a), w) / (a * a);
+    const double den = 1.0 + sv * sv * t;
+    const double e = (sv * sv * (a * w) * (a * w) - 2.0 * v * a * w - v * v * t) / (2.0 * den);
+    return g * exp(e) / sqrt(den);
+}
+
+__device__ __forceinline__ double ddm_logdens64(double rt, const double *p)
+{
+    const double a = p[0], v = p[1], zr = p[2], tshift = p[3], sz = p[4], sv = p[5], st0 = p[6];
+    const int nz = (sz > 0.0) ? kDdmNz : 1;
+    const int nt = (st0 > 0.0) ? kDdmNt : 1;
+    double acc = 0.0;
+    for (int it = 0; it < nt; ++it) {
+        const double tu = (nt > 1) ? tshift + st0 * ((it + 0.5) / nt) : tshift;
+        const double tt = rt - tu;
+        if (!(tt > 0.0)) continue;
+        for (int iz = 0; iz < nz; ++iz) {
+            const double zz = (nz > 1) ? zr + sz * ((iz + 0.5) / nz - 0.5) : zr;
+            acc += ddm_fixed64(tt, a, v, zz, sv);
+        }
+    }
+    double dens = acc / (double)(nz * nt);
+    if (!(dens > 1e-10)) dens = 1e-10;
+    return log(dens);
+}
+
+// FP32 form of the same density: the series lengths from the same bounds
+// evaluated in FP32, the terms and the node sum in FP32.  Returns false
+// (re-evaluate in FP64) below 1e-8, where the 1e-10 floor is near, or when
+// a value is not finite.
+__device__ __forceinline__ float nf_density32(float tt, float w)
+{
+    const float pi = 3.14159265f;
+    float ks, kl;
+    const float ek = pi * tt * 1e-10f;
+    kl = (ek < 1.f) ? fmaxf(sqrtf(-2.f * __logf(ek) / (pi * pi * tt)), 1.f / (pi * sqrtf(tt)))
+                    : 1.f / (pi * sqrtf(tt));
+    const float es = 2.f * sqrtf(2.f * pi * tt) * 1e-10f;
+    ks = (es < 1.f) ? fmaxf(2.f + sqrtf(-2.f * tt * __logf(es)), sqrtf(tt) + 1.f) : 2.f;
+    float p = 0.f;
+    if (ks < kl) {
+        const int K = (int)ceilf(ks);
+        const float i2t = 0.5f / tt;
+        for (int k = -((K - 1) / 2); k <= (K - 1) / 2; ++k) {
+            const float x = w + 2.f * k;
+            p = fmaf(x, expf(-(x * x) * i2t), p);
+        }
+        p *= rsqrtf(2.f * pi * tt * tt * tt);
+    } else {
+        const int K = (int)ceilf(kl);
+        const float c = pi * pi * tt * 0.5f;
+        for (int k = 1; k <= K; ++k) p = fmaf((float)k * expf(-(float)(k * k) * c), sinpif(k * w), p);
+        p *= pi;
+    }
+    return p;
+}
+
+__device__ __forceinline__ bool ddm_logdens32(float rt_hi, float rt_lo, const float *p, float &ld)
+{
+    const float a = p[0], v = p[1], zr = p[2], sz = p[4], sv = p[5], st0 = p[6];
+    const float ia2 = 1.f / (a * a), sv2 = sv * sv;
+    const int nz = (sz > 0.f) ? kDdmNz : 1;
+    const int nt = (st0 > 0.f) ? kDdmNt : 1;
+    float acc = 0.f;
+    for (int it = 0; it < nt; ++it) {
+        // decision time from the (hi, lo) split of rt and tshift (p[3], p[7])
+        const float tu = (nt > 1) ? st0 * ((it + 0.5f) / nt) : 0.f;
+        const float tt = ((rt_hi - p[3]) + (rt_lo - p[7])) - tu;
+        if (!(tt > 0.f)) continue;
+        const float den = fmaf(sv2, tt, 1.f);
+        const float rden = rsqrtf(den), hden = 0.5f / den;
+        float part = 0.f;
+        for (int iz = 0; iz < nz; ++iz) {
+            const float zz = (nz > 1) ? fmaf(sz, (iz + 0.5f) / nz - 0.5f, zr) : zr;
+            const float g = nf_density32(tt * ia2, zz) * ia2;
+            const float aw = a * zz;
+            const float e = (fmaf(sv2 * aw, aw, -2.f * v * aw) - v * v * tt) * hden;
+            part = fmaf(g, expf(e), part);
+        }
+        acc = fmaf(part, rden, acc);
+    }
+    const float dens = acc / (float)(nz * nt);
+    if (!(dens >= 1e-8f) || !(dens < 3.0e38f)) return false;
+    ld = __logf(dens);
+    return true;
+}
+
 }  // namespace ggdmc

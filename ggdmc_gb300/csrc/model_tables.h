@@ -25,6 +25,8 @@ struct EntSrc {
 };
 
 constexpr int kMaxT0 = 255;      // distinct t0 sources (uint8 index)
+constexpr int kMaxDent = 255;    // distinct DDM tuples (uint8 index)
+constexpr int kModelDdm = 1;
 
 struct DevModel {
     int32_t model_type;     // 0 LBA, 1 DDM
@@ -39,7 +41,8 @@ struct DevModel {
     const uint8_t *cell_w;  // [n_cell]         responding accumulator
     const uint8_t *cell_t0; // [n_cell]         index into t0_src
     const int32_t *t0_src;  // [n_t0]           source of each distinct t0
-    const int32_t *ddm_src; // [n_cell][2][8]   DDM parameter sources
+    int32_t n_dent;         // distinct DDM (parameter sources, boundary) tuples
+    const int32_t *ddm_src; // [n_dent][9]      DDM: a, v, z, d, sz, sv, t0, st0 sources + boundary
     const double *consts;   // [n_const]
 };
 

@@ -144,7 +144,7 @@ struct ggdmc_handle {
     int device = 0;
     cudaStream_t stream = nullptr;
     // design
-    int model_type = 0, n_par = 0, n_cell = 0, n_acc = 0, n_ent = 0, n_const = 0;
+    int model_type = 0, n_par = 0, n_cell = 0, n_acc = 0, n_ent = 0, n_const = 0, n_dent = 0;
     DevBuf<EntSrc> ent_src;
     DevBuf<uint8_t> cell_ent, cell_w, cell_t0;
     DevBuf<int32_t> t0_src, ddm_src;
@@ -189,6 +189,7 @@ struct ggdmc_handle {
         m.cell_w = cell_w.p;
         m.cell_t0 = cell_t0.p;
         m.ddm_src = ddm_src.p;
+        m.n_dent = n_dent;
         m.consts = consts.p;
         return m;
     }
@@ -234,11 +235,67 @@ ggdmc_status wait_stream(cudaStream_t st)
     return GGDMC_OK;
 }
 
+// Diffusion model: two boundaries; the density of a cell depends only on the
+// responding boundary's 8 parameters, so cells with equal (sources, boundary)
+// share one entry.
+ggdmc_status build_design_ddm(ggdmc_handle *h, const ggdmc_model *m)
+{
+    if (m->n_kind != GGDMC_DDM_NKIND) return fail(GGDMC_ERR_ARG, "DDM model needs n_kind == 8");
+    if (m->n_acc != 2) return fail(GGDMC_ERR_ARG, "DDM model needs n_acc == 2 (two boundaries)");
+    if (m->n_par < 1 || m->n_par > kMaxPar) return fail(GGDMC_ERR_ARG, "n_par out of range (1..64)");
+    if (m->n_cell < 1 || m->n_cell > kMaxCell) return fail(GGDMC_ERR_ARG, "n_cell out of range");
+    if (m->n_const < 0 || (m->n_const > 0 && !m->constants))
+        return fail(GGDMC_ERR_ARG, "constants missing");
+    std::map<std::vector<int32_t>, int> uniq;
+    std::vector<int32_t> dsrc;
+    std::vector<uint8_t> cent((size_t)m->n_cell * 2), cw(m->n_cell), ct0(m->n_cell, 0);
+    for (int c = 0; c < m->n_cell; ++c) {
+        const int w = m->resp[c];
+        if (w < 0 || w > 1) return fail(GGDMC_ERR_ARG, "DDM resp must be 0 (lower) or 1 (upper)");
+        std::vector<int32_t> key(m->param_src + ((size_t)c * 2 + w) * 8,
+                                 m->param_src + ((size_t)c * 2 + w) * 8 + 8);
+        for (int32_t q : key)
+            if (!((q >= 0 && q < m->n_par) || (q < 0 && -1 - q < m->n_const)))
+                return fail(GGDMC_ERR_ARG, "parameter source out of range");
+        key.push_back(w);
+        auto it = uniq.find(key);
+        int id;
+        if (it == uniq.end()) {
+            id = (int)uniq.size();
+            if (id >= kMaxDent) return fail(GGDMC_ERR_ARG, "too many distinct DDM cells");
+            uniq[key] = id;
+            dsrc.insert(dsrc.end(), key.begin(), key.end());
+        } else {
+            id = it->second;
+        }
+        cent[(size_t)c * 2] = cent[(size_t)c * 2 + 1] = (uint8_t)id;
+        cw[c] = (uint8_t)w;
+    }
+    h->model_type = GGDMC_MODEL_DDM;
+    h->n_par = m->n_par;
+    h->n_cell = m->n_cell;
+    h->n_acc = 2;
+    h->n_ent = 0;
+    h->n_t0 = 0;
+    h->n_dent = (int)uniq.size();
+    h->n_const = m->n_const;
+    std::vector<double> consts(m->constants, m->constants + m->n_const);
+    if (consts.empty()) consts.push_back(0.0);
+    cudaStream_t st = h->stream;
+    CU(h->ddm_src.upload(dsrc.data(), dsrc.size(), st));
+    CU(h->cell_ent.upload(cent.data(), cent.size(), st));
+    CU(h->cell_w.upload(cw.data(), cw.size(), st));
+    CU(h->cell_t0.upload(ct0.data(), ct0.size(), st));
+    CU(h->consts.upload(consts.data(), consts.size(), st));
+    CU(configure_kernels(h->dev_model()));
+    return GGDMC_OK;
+}
+
 ggdmc_status build_design(ggdmc_handle *h, const ggdmc_model *m)
 {
     if (!m || !m->param_src || !m->resp) return fail(GGDMC_ERR_ARG, "model is NULL or incomplete");
-    if (m->model_type != GGDMC_MODEL_LBA)
-        return fail(GGDMC_ERR_ARG, "only the LBA model runs on this build");
+    if (m->model_type == GGDMC_MODEL_DDM) return build_design_ddm(h, m);
+    if (m->model_type != GGDMC_MODEL_LBA) return fail(GGDMC_ERR_ARG, "unknown model_type");
     if (m->n_kind != GGDMC_LBA_NKIND) return fail(GGDMC_ERR_ARG, "LBA model needs n_kind == 6");
     if (m->n_par < 1 || m->n_par > kMaxPar) return fail(GGDMC_ERR_ARG, "n_par out of range (1..64)");
     if (m->n_cell < 1 || m->n_cell > kMaxCell) return fail(GGDMC_ERR_ARG, "n_cell out of range");

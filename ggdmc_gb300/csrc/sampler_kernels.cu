@@ -311,11 +311,13 @@ struct SubSmem {
     uint8_t *cw;     // n_cell
     uint8_t *ct0;    // n_cell
     int *flag;       // [kGroup] 1: FP32 form unusable for proposal g
+    double *d64;     // [kGroup][n_dent][8] DDM entries (FP64)
+    float *d32;      // [kGroup][n_dent][8] DDM entries (FP32; [3],[7] tshift hi, lo)
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[11])
+__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[13])
 {
     size_t o = 0;
     off[0] = o; o += sizeof(double) * kMaxTheta * kGroup;
@@ -331,18 +333,21 @@ __host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[
     off[9] = o; o += m.n_cell;
     o = align_up(o, 16);
     off[10] = o; o += sizeof(int) * kGroup;
+    o = align_up(o, 16);
+    off[11] = o; o += sizeof(double) * 8 * m.n_dent * kGroup;
+    off[12] = o; o += sizeof(float) * 8 * m.n_dent * kGroup;
     return align_up(o, 16);
 }
 
 __host__ __device__ size_t sub_smem_bytes(const DevModel &m)
 {
-    size_t off[11];
+    size_t off[13];
     return sub_smem_layout(m, off);
 }
 
 __device__ SubSmem carve(char *base, const DevModel &m)
 {
-    size_t off[11];
+    size_t off[13];
     sub_smem_layout(m, off);
     SubSmem s;
     s.theta = (double *)(base + off[0]);
@@ -356,6 +361,8 @@ __device__ SubSmem carve(char *base, const DevModel &m)
     s.cw = (uint8_t *)(base + off[8]);
     s.ct0 = (uint8_t *)(base + off[9]);
     s.flag = (int *)(base + off[10]);
+    s.d64 = (double *)(base + off[11]);
+    s.d32 = (float *)(base + off[12]);
     return s;
 }
 
@@ -456,9 +463,71 @@ __device__ __forceinline__ double trial64(const RunDev &r, const SubSmem &sm, in
 // threads.  MIXED: FP32 per trial, each trial's data read once for the whole
 // group; FP64 tables are built only for a proposal some trial of which needs
 // the FP64 form, and only those trials use it.
+// DDM entries of proposal g from its theta (the responding boundary's
+// mirrored values; see ddm_logdens64).
+__device__ void ddm_build(const RunDev &r, SubSmem &sm, int g, const double *theta)
+{
+    const int ND = r.m.n_dent;
+    for (int u = threadIdx.x; u < ND; u += blockDim.x) {
+        const int32_t *q = r.m.ddm_src + 9 * u;
+        double v8[8];
+        for (int j = 0; j < 8; ++j) v8[j] = src_value(q[j], theta, r.m.consts);
+        const bool upper = q[8] == 1;
+        double *e = sm.d64 + 8 * (g * ND + u);
+        e[0] = v8[0];
+        e[1] = upper ? -v8[1] : v8[1];
+        e[2] = upper ? 1.0 - v8[2] : v8[2];
+        e[3] = upper ? v8[6] - v8[3] / 2.0 : v8[6] + v8[3] / 2.0;
+        e[4] = v8[4];
+        e[5] = v8[5];
+        e[6] = v8[7];
+        e[7] = 0.0;
+        float *f = sm.d32 + 8 * (g * ND + u);
+        for (int j = 0; j < 7; ++j) f[j] = (float)e[j];
+        f[7] = (float)(e[3] - (double)f[3]);
+    }
+}
+
+// group_loglik for the diffusion model: FP32 per trial (MIXED) with FP64
+// re-evaluation where ddm_logdens32 declines, or FP64 throughout.
+__device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed,
+                                 double *out)
+{
+    for (int g = 0; g < ng; ++g) ddm_build(r, sm, g, sm.theta + g * kMaxTheta);
+    __syncthreads();
+    const int64_t base = r.offs[l] + i0;
+    const int n = i1 - i0, K = r.m.n_acc, ND = r.m.n_dent;
+    double acc[kGroup];
+    float ks[kGroup], kc[kGroup];
+#pragma unroll
+    for (int g = 0; g < kGroup; ++g) { acc[g] = 0.0; ks[g] = 0.f; kc[g] = 0.f; }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int u = sm.cent[r.cell[base + i] * K];
+        const float2 rt = r.rt32[base + i];
+#pragma unroll
+        for (int g = 0; g < kGroup; ++g) {
+            if (g >= ng) break;
+            float ld;
+            if (mixed && ddm_logdens32(rt.x, rt.y, sm.d32 + 8 * (g * ND + u), ld)) {
+                const float y = ld - kc[g];
+                const float tt = ks[g] + y;
+                kc[g] = (tt - ks[g]) - y;
+                ks[g] = tt;
+            } else {
+                acc[g] += ddm_logdens64(r.rt64[base + i], sm.d64 + 8 * (g * ND + u));
+            }
+        }
+    }
+    for (int g = 0; g < ng; ++g) out[g] = block_sum(acc[g] + ((double)ks[g] - (double)kc[g]), sm.red);
+}
+
 __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed,
                              double *out)
 {
+    if (r.m.model_type == kModelDdm) {
+        ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, out);
+        return;
+    }
     const int64_t base = r.offs[l] + i0;
     const int n = i1 - i0;
     const int K = r.m.n_acc;
@@ -1735,12 +1804,25 @@ __global__ void __launch_bounds__(kLikThreads) k_trial_logdens(RunDev r, const d
     if (threadIdx.x == 0) sm.flag[0] = 0;
     __syncthreads();
     const bool mixed = r.prec == PREC_MIXED;
-    if (mixed) build_tables32(r, sm, 0);
-    build_tables64(r, sm, sm.theta);
-    __syncthreads();
     const int64_t base = r.offs[l];
     const int n = (int)(r.offs[l + 1] - base);
     const int K = r.m.n_acc;
+    if (r.m.model_type == kModelDdm) {
+        ddm_build(r, sm, 0, sm.theta);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int u = sm.cent[r.cell[base + i] * K];
+            const float2 rt = r.rt32[base + i];
+            float ld;
+            out[base + i] = (mixed && ddm_logdens32(rt.x, rt.y, sm.d32 + 8 * u, ld))
+                                ? (double)ld
+                                : ddm_logdens64(r.rt64[base + i], sm.d64 + 8 * u);
+        }
+        return;
+    }
+    if (mixed) build_tables32(r, sm, 0);
+    build_tables64(r, sm, sm.theta);
+    __syncthreads();
     const bool use32 = mixed && sm.flag[0] == 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int c = r.cell[base + i];

@@ -24,7 +24,7 @@ import itertools
 
 import numpy as np
 
-from .dmi import LBA_KINDS, MODEL_LBA, FlatModel
+from .dmi import DDM_KINDS, LBA_KINDS, MODEL_DDM, MODEL_LBA, FlatModel
 
 
 def _param_name(q, facs, levels, acc, match_factor, match_map):
@@ -147,6 +147,26 @@ T0_17_P = {
     "mean_v.red.true": 2.5, "mean_v.yellow.true": 2.7, "mean_v.blue.true": 2.9,
     "mean_v.green.true": 3.1, "mean_v.red.false": 1.24, "mean_v.yellow.false": 1.52,
     "mean_v.blue.false": 1.44, "mean_v.green.false": 1.72, "sd_v.true": 0.2}
+
+
+def design_ddm9() -> FlatModel:
+    """Ratcliff diffusion design with 9 parameters: a, v per stimulus (2
+    levels), z, d, sz, sv, t0, st0 (z and sz relative to a).  Two responses:
+    r1 is the lower boundary, r2 the upper; cells are stimulus x response."""
+    pnames = ["a", "v.s1", "v.s2", "z", "d", "sz", "sv", "t0", "st0"]
+    accs = ["r1", "r2"]
+    cells = [f"{st}.{rsp}" for st in ("s1", "s2") for rsp in accs]
+    src = np.zeros((len(cells), 2, len(DDM_KINDS)), np.int32)
+    for c, name in enumerate(cells):
+        st = name.split(".")[0]
+        src[c, :, :] = [pnames.index(k) for k in ("a", f"v.{st}", "z", "d", "sz", "sv", "t0", "st0")]
+    resp = np.array([accs.index(n.split(".")[1]) for n in cells], np.int32)
+    return FlatModel(MODEL_DDM, pnames, accs, cells, np.zeros(0), [], src, resp, DDM_KINDS)
+
+
+# population values of the diffusion design (rtdists-style magnitudes)
+DDM9_P = {"a": 1.0, "v.s1": -1.5, "v.s2": 1.5, "z": 0.5, "d": 0.02, "sz": 0.2, "sv": 0.5,
+          "t0": 0.3, "st0": 0.15}
 
 
 def vector(model: FlatModel, values: dict) -> np.ndarray:

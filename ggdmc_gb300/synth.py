@@ -14,7 +14,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .design import (BV13_POP_MEAN, BV13_POP_SCALE, T0_17_P, design_bv13, design_rows,
+from .design import (BV13_POP_MEAN, BV13_POP_SCALE, DDM9_P, T0_17_P, design_bv13, design_ddm9,
+                     design_rows,
                      design_t0_17, vector)
 from .dmi import FlatModel, SubjectBatch, SubjectData
 
@@ -136,6 +137,82 @@ def many_fits_1024(seed: int = 4, n_fit: int = 1024, n_lo: int = 200, n_hi: int 
     P = model.n_par
     return Workload("many_fits_1024", model, SubjectBatch.pack(subs), np.array(thetas),
                     unif_prior(P), None, None, None, 3 * P, False)
+
+
+def simulate_ddm_batch(model: FlatModel, thetas: np.ndarray, ns, rng, dt: float = 1e-4,
+                       tmax: float = 5.0) -> list:
+    """Diffusion trials by Euler integration of the unit-variance Wiener
+    process, every subject's trials advanced together: start a (z + sz (U -
+    1/2)), drift ~ N(v, sv^2), absorbed at 0 (response r1) or a (r2);
+    RT = decision time + t0 + st0 U, -d/2 for the upper response, +d/2 for
+    the lower.  Stimuli are equally likely.  Trials still running at tmax
+    are dropped."""
+    stimuli = sorted({c.split(".")[0] for c in model.cell_names})
+    kidx = {k: i for i, k in enumerate(model.kinds)}
+    subj, stim, par = [], [], []
+    for s, (th, n) in enumerate(zip(thetas, ns)):
+        cv = model.cell_values(th)                      # [n_cell, 2, 8]
+        st = rng.integers(0, len(stimuli), int(n))
+        rows = np.array([model.cell_names.index(f"{stimuli[k]}.{model.accumulators[0]}") for k in st])
+        subj.append(np.full(int(n), s))
+        stim.append(st)
+        par.append(cv[rows, 0, :])
+    subj, stim, par = np.concatenate(subj), np.concatenate(stim), np.concatenate(par)
+    g = lambda k: par[:, kidx[k]]
+    a, v, z, d, sz, sv, t0, st0 = (g(k) for k in ("a", "v", "z", "d", "sz", "sv", "t0", "st0"))
+    x = a * (z + sz * (rng.random(len(a)) - 0.5))
+    drift = v + sv * rng.standard_normal(len(a))
+    tdec = np.full(len(a), np.nan)
+    resp = np.full(len(a), -1)
+    act = np.arange(len(a))
+    sq = np.sqrt(dt)
+    for step in range(1, int(tmax / dt) + 1):
+        x[act] += drift[act] * dt + sq * rng.standard_normal(len(act))
+        lo, hi = x[act] <= 0.0, x[act] >= a[act]
+        done = lo | hi
+        if done.any():
+            idx = act[done]
+            tdec[idx] = step * dt
+            resp[idx] = np.where(hi[done], 1, 0)
+            act = act[~done]
+        if len(act) == 0:
+            break
+    tnd = t0 + st0 * rng.random(len(a)) + np.where(resp == 1, -d / 2, d / 2)
+    rt = tdec + tnd
+    out = []
+    for s in range(len(ns)):
+        m = (subj == s) & (resp >= 0)
+        cells = np.array([model.cell_names.index(f"{stimuli[k]}.{model.accumulators[r]}")
+                          for k, r in zip(stim[m], resp[m])], np.int32)
+        order = np.argsort(cells, kind="stable")           # cell-grouped, as dmi@data
+        out.append(SubjectData(rt[m][order], cells[order], str(s + 1)))
+    return out
+
+
+def hier_ddm_64(seed: int = 3, n_subject: int = 64, n: int = 500, dt: float = 1e-4) -> Workload:
+    """64 subjects x 500 diffusion trials (Euler, dt = 1e-4 s) of the
+    9-parameter design; subject theta ~ N(pop, 10% CV), positive kinds
+    truncated at 0; 27 chains (3 x npar)."""
+    rng = np.random.default_rng(seed)
+    model = design_ddm9()
+    pop = vector(model, DDM9_P)
+    sc = 0.1 * np.abs(pop)
+    signed = np.array([nm.startswith("v.") for nm in model.pnames])
+    thetas = []
+    for _ in range(n_subject):
+        th = pop + sc * rng.standard_normal(len(pop))
+        th = np.where(signed, th, np.abs(th))
+        thetas.append(th)
+    thetas = np.array(thetas)
+    subs = simulate_ddm_batch(model, thetas, [n] * n_subject, rng, dt)
+    P = model.n_par
+    lo = np.where(signed, -np.inf, 0.0)
+    hi = np.array([1.0 if nm in ("z", "sz") else np.inf for nm in model.pnames])
+    p_prior = np.stack([pop, np.full(P, 2.0), lo, hi, np.ones(P), np.ones(P)], axis=1)
+    h_loc = np.stack([pop, np.full(P, 2.0), lo, hi, np.ones(P), np.ones(P)], axis=1)
+    h_prior = np.concatenate([h_loc, unif_prior(P, 0.0, 5.0)])
+    return Workload("hier_ddm_64", model, SubjectBatch.pack(subs), thetas, p_prior, h_prior,
+                    pop, sc, 3 * P, True)
 
 
 def start_states(w: Workload, nchain: int, rng, spread: float = 0.05):

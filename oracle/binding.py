@@ -82,6 +82,13 @@ def sumloglike(model, rt, cell, theta, per_trial=False):
     return (s, pt[:len(rt)].copy()) if per_trial else s
 
 
+def ddm_dens(rt, cv, w):
+    """Diffusion density of one trial: cv [2][8] (a, v, z, d, sz, sv, t0,
+    st0) per boundary, w = 0 lower, 1 upper (floored at 1e-10)."""
+    cv = np.ascontiguousarray(cv, np.float64).reshape(-1)
+    return lib().oracle_ddm_dens(float(rt), abi.dptr(cv), int(w))
+
+
 def loglik(model, batch, theta):
     """theta [S][n][P] -> [S][n]."""
     m = abi.Marshal()
