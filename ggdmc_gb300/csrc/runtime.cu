@@ -143,6 +143,8 @@ ggdmc_status prior_rows(const ggdmc_prior *p, std::vector<double> &rows)
 struct ggdmc_handle {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;       // the subject branch of a hierarchical sweep
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // design
     int model_type = 0, n_par = 0, n_cell = 0, n_acc = 0, n_ent = 0, n_const = 0, n_dent = 0;
     DevBuf<EntSrc> ent_src;
@@ -632,6 +634,19 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     // One DE iteration (src/de.cpp:201-242 / 272-383) as a launch sequence.
     auto one_iteration = [&]() -> cudaError_t {
         cudaError_t e;
+        // Hierarchical and batched: the first subject pass's proposals and
+        // their speculative evaluation read nothing the phi level writes
+        // (only their priors do), so they run on a second stream beside it;
+        // k_sub_prior scores the priors after the join.
+        const bool fork = hier && S > 0 && Pphi > 0 && !plain;
+        if (fork) {
+            if ((e = cudaEventRecord(h->ev_fork, st))) return e;
+            if ((e = cudaStreamWaitEvent(h->stream2, h->ev_fork, 0))) return e;
+            if ((e = launch_sub_propose(r, 0, true, h->stream2))) return e;
+            if ((e = launch_sub_loglik(r, h->items.p, n_spec_items, spec_group, h->stream2))) return e;
+            if ((e = cudaEventRecord(h->ev_join, h->stream2))) return e;
+            launches_per_iter += 2;
+        }
         if (Pphi > 0) {
             const int npass = hier ? (c.is_hblocked ? c.nparameter : 1)
                                    : (c.is_pblocked ? c.nparameter : 1);
@@ -650,7 +665,14 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             const int npass = hier ? (c.is_pblocked ? c.nparameter / 2 : 1)
                                    : (c.is_pblocked ? c.nparameter : 1);
             for (int p = 0; p < npass; ++p) {
-                if ((e = launch_sub_propose(r, p, st))) return e;
+                if (fork && p == 0) {
+                    if ((e = cudaStreamWaitEvent(st, h->ev_join, 0))) return e;
+                    if ((e = launch_sub_prior(r, st))) return e;
+                    if ((e = launch_sub_resolve(r, 0, 0, S, st))) return e;
+                    launches_per_iter += 2;
+                    continue;
+                }
+                if ((e = launch_sub_propose(r, p, false, st))) return e;
                 ++launches_per_iter;
                 if (plain) {
                     for (int l = 0; l < S; ++l) {
@@ -828,6 +850,16 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     return GGDMC_OK;
 }
 
+void release_streams(ggdmc_handle *h)
+{
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->stream2) cudaStreamSynchronize(h->stream2);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->stream2) cudaStreamDestroy(h->stream2);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
 ggdmc_status make_handle(const ggdmc_model *model, const ggdmc_data *data, ggdmc_handle **out)
 {
     if (!out) return fail(GGDMC_ERR_ARG, "out is NULL");
@@ -840,15 +872,16 @@ ggdmc_status make_handle(const ggdmc_model *model, const ggdmc_data *data, ggdmc
     cudaGetDevice(&h->device);
     cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
     if (h->n_sm < 1) h->n_sm = 1;
-    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) {
-        delete h;
-        return fail(GGDMC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
-    }
-    ggdmc_status s = GGDMC_OK;
-    if (model) s = build_design(h, model);
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (!e) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+    if (!e) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    ggdmc_status s = e ? fail(GGDMC_ERR_CUDA, std::string("stream / event create: ") + cudaGetErrorString(e))
+                       : GGDMC_OK;
+    if (!s && model) s = build_design(h, model);
     if (!s) s = upload_data(h, data);
     if (s) {
-        cudaStreamDestroy(h->stream);
+        release_streams(h);
         delete h;
         return s;
     }
@@ -894,8 +927,7 @@ ggdmc_status ggdmc_create(const ggdmc_model *model, const ggdmc_data *data, ggdm
 ggdmc_status ggdmc_destroy(ggdmc_handle *h)
 {
     if (!h) return GGDMC_OK;
-    cudaStreamSynchronize(h->stream);
-    cudaStreamDestroy(h->stream);
+    release_streams(h);
     delete h;
     return GGDMC_OK;
 }

@@ -103,7 +103,8 @@ struct RunDev {
 
 // --------------------------------------------------------------- launchers
 // (defined in sampler_kernels.cu)
-cudaError_t launch_sub_propose(const RunDev &r, int pass, cudaStream_t st);
+cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, cudaStream_t st);
+cudaError_t launch_sub_prior(const RunDev &r, cudaStream_t st);
 cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, int group,
                               cudaStream_t st);
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,

@@ -665,7 +665,18 @@ __device__ __forceinline__ double warp_prior(const RunDev &r, const double *th, 
 // k_sub_propose: pass type, partners, stored draws and proposals of every
 // chain of every subject level, with their log priors and FP32 tables.
 // grid = S.
-__global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int pass)
+// In a hierarchical sweep the subject proposals are built while the phi
+// level runs (defer_prior): the prior, the only term that reads phi, is
+// scored after both by k_sub_prior, and a proposal is evaluated when it lies
+// in the prior's support, which does not depend on phi.
+__device__ __forceinline__ bool in_support(const RunDev &r, const double *th)
+{
+    for (int j = 0; j < r.P; ++j)
+        if (!(th[j] >= r.pp_bounds[2 * j] && th[j] <= r.pp_bounds[2 * j + 1])) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int pass, int defer_prior)
 {
     __shared__ double s_u[kMaxChain + 2];
     __shared__ int s_sub[kMaxChain];
@@ -750,13 +761,20 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
     }
     __syncthreads();
     const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int k = wid; k < n; k += nw) {
-        const int owner = (type == PASS_CROSS) ? k : s_sub[k];
-        const double lp = warp_prior(r, ths + (size_t)k * P, owner);
-        if ((threadIdx.x & 31) == 0) {
-            r.lp_s[(size_t)l * CS + k] = lp;
+    if (defer_prior) {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
             r.ll_s[(size_t)l * CS + k] = 0.0;
-            r.need[(size_t)l * CS + k] = (lp > -INFINITY) ? 1 : 0;
+            r.need[(size_t)l * CS + k] = in_support(r, ths + (size_t)k * P) ? 1 : 0;
+        }
+    } else {
+        for (int k = wid; k < n; k += nw) {
+            const int owner = (type == PASS_CROSS) ? k : s_sub[k];
+            const double lp = warp_prior(r, ths + (size_t)k * P, owner);
+            if ((threadIdx.x & 31) == 0) {
+                r.lp_s[(size_t)l * CS + k] = lp;
+                r.ll_s[(size_t)l * CS + k] = 0.0;
+                r.need[(size_t)l * CS + k] = (lp > -INFINITY) ? 1 : 0;
+            }
         }
     }
     // migration: the cascade V_s = V_(s-1) + jit_s from V_0 = proposal 0, the
@@ -788,13 +806,22 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
         }
         for (int w = threadIdx.x; w < nv; w += blockDim.x) r.tab_bad[(size_t)l * CS + C + w] = 0;
         __syncthreads();
-        for (int w = wid; w < nv; w += nw) {
+        if (defer_prior) {
             // V_0 equals proposal 0, already evaluated
-            const double lp = (w == 0) ? -INFINITY : warp_prior(r, ths + (size_t)(C + w) * P, s_sub[w]);
-            if ((threadIdx.x & 31) == 0) {
-                r.lp_s[(size_t)l * CS + C + w] = lp;
+            for (int w = threadIdx.x; w < nv; w += blockDim.x) {
                 r.ll_s[(size_t)l * CS + C + w] = 0.0;
-                r.need[(size_t)l * CS + C + w] = (lp > -INFINITY) ? 1 : 0;
+                r.need[(size_t)l * CS + C + w] =
+                    (w > 0 && in_support(r, ths + (size_t)(C + w) * P)) ? 1 : 0;
+            }
+        } else {
+            for (int w = wid; w < nv; w += nw) {
+                // V_0 equals proposal 0, already evaluated
+                const double lp = (w == 0) ? -INFINITY : warp_prior(r, ths + (size_t)(C + w) * P, s_sub[w]);
+                if ((threadIdx.x & 31) == 0) {
+                    r.lp_s[(size_t)l * CS + C + w] = lp;
+                    r.ll_s[(size_t)l * CS + C + w] = 0.0;
+                    r.need[(size_t)l * CS + C + w] = (lp > -INFINITY) ? 1 : 0;
+                }
             }
         }
     }
@@ -810,6 +837,26 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
 // k_sub_loglik: the hot kernel.  One CTA per work item = up to kGroup
 // proposals of one subject, items in descending trial-count order (longest
 // first keeps the tail short).  item = level * CS + first slot.
+// k_sub_prior: the deferred priors of a pass's proposals (and of the
+// migration cascade), a warp per slot, with the phi chains of this sweep.
+__global__ void __launch_bounds__(kProposeThreads) k_sub_prior(RunDev r)
+{
+    const int l = blockIdx.x;
+    const int type = r.ptype[l], n = r.nstep[l];
+    if (type == PASS_SKIP || n == 0) return;
+    const int C = r.C, P = r.P, CS = r.CS;
+    const double *ths = r.th_s + (size_t)l * CS * P;
+    const int nv = (type == PASS_MIG) ? n : 0;
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = wid; q < n + nv; q += nw) {
+        const int slot = (q < n) ? q : C + (q - n);
+        const int k = (q < n) ? q : q - n;
+        const int owner = (type == PASS_CROSS) ? k : r.sub[(size_t)l * C + k];
+        const double lp = (slot == C) ? -INFINITY : warp_prior(r, ths + (size_t)slot * P, owner);
+        if ((threadIdx.x & 31) == 0) r.lp_s[(size_t)l * CS + slot] = lp;
+    }
+}
+
 __global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int32_t *items, int group)
 {
     extern __shared__ __align__(16) char smem_raw[];
@@ -1878,9 +1925,15 @@ cudaError_t configure_kernels(const DevModel &m)
     return cudaFuncSetAttribute(k_trial_logdens, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t launch_sub_propose(const RunDev &r, int pass, cudaStream_t st)
+cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, cudaStream_t st)
 {
-    k_sub_propose<<<r.S, kProposeThreads, 0, st>>>(r, pass);
+    k_sub_propose<<<r.S, kProposeThreads, 0, st>>>(r, pass, defer_prior ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_prior(const RunDev &r, cudaStream_t st)
+{
+    k_sub_prior<<<r.S, kProposeThreads, 0, st>>>(r);
     return cudaGetLastError();
 }
 
