@@ -833,8 +833,12 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         }
     }
     unsigned long long hs[ST_N];
+    int32_t dev_status = 0;
     CU(cudaMemcpyAsync(hs, h->stats.p, sizeof hs, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&dev_status, h->status.p, sizeof dev_status, cudaMemcpyDeviceToHost, st));
     if ((s = wait_stream(st))) return s;
+    if (dev_status)
+        return fail(GGDMC_ERR_TIMEOUT, "a device-side wait gave up (code " + std::to_string(dev_status) + ")");
     if (a.stats) {
         a.stats->proposals = (int64_t)hs[ST_PROPOSALS];
         a.stats->accepts = (int64_t)hs[ST_ACCEPTS];

@@ -32,6 +32,7 @@ enum StatIdx { ST_PROPOSALS = 0, ST_ACCEPTS, ST_MIGRATIONS, ST_REEVALS, ST_TRIAL
 // proposals.
 constexpr int kVariants = 8;
 
+
 struct RunDev {
     // ------------------------------------------------------------ shape
     int32_t C;            // chains

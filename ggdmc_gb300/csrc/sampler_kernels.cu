@@ -18,22 +18,26 @@
 // one the sequential algorithm would have built, and re-proposes and
 // re-evaluates the rest round by round.  Given the same draws the accepted
 // states equal the sequential sampler's.
+#include <algorithm>
 #include <cfloat>
 #include <cstdio>
 #include <cstdint>
 
-#include <cooperative_groups.h>
-
 #include "sampler.cuh"
+
+// k_sub_resolve's block: 512 threads, one CTA per SM (128 registers a thread;
+// measured faster than 384 x 2 and 768 x 1 on the 256-subject workload)
+#ifndef GGDMC_RESOLVE_THREADS
+#define GGDMC_RESOLVE_THREADS 512
+#endif
+#ifndef GGDMC_RESOLVE_MINB
+#define GGDMC_RESOLVE_MINB 1
+#endif
 
 namespace ggdmc {
 
 constexpr int kLikThreads = 128;
-constexpr int kResolveThreads = 384;
-#ifndef GGDMC_RESOLVE_CLUSTER
-#define GGDMC_RESOLVE_CLUSTER 1
-#endif
-constexpr int kResolveCluster = GGDMC_RESOLVE_CLUSTER;   // CTAs per subject in resolve
+constexpr int kResolveThreads = GGDMC_RESOLVE_THREADS;
 constexpr int kMigRound = 8;              // migration variants evaluated per resolve round
 constexpr int kPhiThreads = 256;
 constexpr int kProposeThreads = 512;
@@ -879,48 +883,27 @@ __global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int3
     eval_slots(r, l, s_slots, s_m, sm, r.prec == PREC_MIXED, nullptr);
 }
 
-// Barrier of the resolve cluster (a block barrier when it has one CTA); it
-// orders shared and global memory across the cluster's CTAs.
-__device__ __forceinline__ void cluster_barrier()
+// Evaluate slots[0..m) of subject l over all its trials, kGroup at a time;
+// out[slots[q] - out_off] and ll_s receive slot q's log-likelihood.
+__device__ void eval_direct(const RunDev &r, int l, const int *slots, int m, SubSmem &sm, bool mixed,
+                            double *out, int out_off)
 {
-    if constexpr (kResolveCluster == 1) __syncthreads();
-    else cooperative_groups::this_cluster().sync();
-}
-
-// eval_slots across a cluster: each CTA sums its slice of the subject's
-// trials, the partials are exchanged through distributed shared memory and
-// every CTA adds them in rank order, so all CTAs hold identical totals.
-// out[slots[q] - out_off] = total of slot q; the lead CTA also stores ll_s.
-__device__ void eval_slots_cluster(const RunDev &r, int l, const int *slots, int m, SubSmem &sm, bool mixed,
-                                   double *part, double *out, int out_off, bool lead)
-{
-    namespace cg = cooperative_groups;
-    cg::cluster_group cl = cg::this_cluster();
-    const int Q = kResolveCluster, rank = (int)cl.block_rank();
     const int N = (int)(r.offs[l + 1] - r.offs[l]);
-    const int i0 = (int)((int64_t)N * rank / Q), i1 = (int)((int64_t)N * (rank + 1) / Q);
     for (int g0 = 0; g0 < m; g0 += kGroup) {
         const int ng = min(kGroup, m - g0);
         for (int g = 0; g < ng; ++g) load_slot(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
         __syncthreads();
         double o[kGroup];
-        group_loglik(r, l, i0, i1, sm, ng, mixed, o);
+        group_loglik(r, l, 0, N, sm, ng, mixed, o);
         if (threadIdx.x == 0) {
-            for (int g = 0; g < ng; ++g) part[g0 + g] = o[g];
-            atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)(i1 - i0) * ng);
+            for (int g = 0; g < ng; ++g) {
+                out[slots[g0 + g] - out_off] = o[g];
+                r.ll_s[(size_t)l * r.CS + slots[g0 + g]] = o[g];
+            }
+            atomicAdd(&r.stats[ST_TRIALS], (unsigned long long)N * ng);
         }
         __syncthreads();
     }
-    cluster_barrier();
-    for (int q = threadIdx.x; q < m; q += blockDim.x) {
-        double t = 0.0;
-        if constexpr (kResolveCluster == 1) t = part[q];
-        else
-            for (int k = 0; k < Q; ++k) t += cl.map_shared_rank(part, k)[q];
-        out[slots[q] - out_off] = t;
-        if (lead) r.ll_s[(size_t)l * r.CS + slots[q]] = t;
-    }
-    cluster_barrier();   // partials are read before any CTA overwrites them
 }
 
 struct ResSmem {
@@ -1011,39 +994,25 @@ __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &
     __syncthreads();
 }
 
-// k_sub_resolve: ordered decisions of one subject level per cluster
-// (src/de.cpp:111-199, 567-665).  Decisions are taken from the speculative
-// results while the proposal a step would get in sequence is the one
-// evaluated; a crossover chain whose partner moved earlier in the sweep is
-// re-proposed from the current state and re-evaluated with the other stale
-// chains of its round.  Migration steps: the first round uses the start-of-
-// pass proposals (valid after a rejection) and the cascade from step 0 (valid
-// while every step accepts); later rounds evaluate the most likely values
-// the next steps can need.  With a cluster of several CTAs each CTA takes
-// the same decisions and evaluates a slice of the trials; the lead CTA alone
-// writes the chain state.
-#if GGDMC_RESOLVE_CLUSTER > 1
-#define GGDMC_RESOLVE_CLUSTER_DIMS __cluster_dims__(GGDMC_RESOLVE_CLUSTER, 1, 1)
-#else
-#define GGDMC_RESOLVE_CLUSTER_DIMS
-#endif
-__global__ void GGDMC_RESOLVE_CLUSTER_DIMS __launch_bounds__(kResolveThreads, 2)
-k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
+// resolve_level: ordered decisions of one subject level (src/de.cpp:111-199,
+// 567-665), by one CTA.  Decisions are taken from the speculative results
+// while the proposal a step would get in sequence is the one evaluated; a
+// crossover chain whose partner moved earlier in the sweep is re-proposed
+// from the current state and re-evaluated with the other stale chains of its
+// round.  Migration steps: the first round uses the start-of-pass proposals
+// (valid after a rejection) and the cascade from step 0 (valid while every
+// step accepts); later rounds evaluate the most likely values the next steps
+// can need.
+__device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_raw)
 {
-    const int rank = (kResolveCluster == 1) ? 0 : (int)cooperative_groups::this_cluster().block_rank();
-    const bool lead = rank == 0;
-    const int slot_in_grid = blockIdx.x / kResolveCluster;
-    const int l = level_begin + (order ? order[slot_in_grid] : slot_in_grid);
-    extern __shared__ __align__(16) char smem_raw[];
+    const bool lead = true;
     const int type = r.ptype[l];
-    if (type == PASS_SKIP) return;   // uniform across the cluster
+    if (type == PASS_SKIP) return;
     const int n = r.nstep[l];
     const int C = r.C, P = r.P;
     const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
     const bool mixed = r.prec == PREC_MIXED;
-    SubSmem sm = carve(smem_raw, r.m);
     ResSmem rs = carve_res(smem_raw + sub_smem_bytes(r.m), C);
-    load_design(r, sm);
     for (int k = threadIdx.x; k < C; k += blockDim.x) {
         rs.lp[k] = r.lp[lc + k];
         rs.ll[k] = r.ll[lc + k];
@@ -1071,8 +1040,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
         __syncthreads();
         jit = js;
     }
-    // work split of the re-proposals across the cluster
-    const int ct = rank * blockDim.x + threadIdx.x, cstride = kResolveCluster * blockDim.x;
+    const int ct = threadIdx.x, cstride = blockDim.x;
     int rounds = 0, reevals = 0, variants = 0;
     int decided = 0;
 #ifdef GGDMC_PHASE_PROFILE
@@ -1122,7 +1090,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
                 }
                 rs.misc[2] = m;
             }
-            cluster_barrier();   // the lead's accepted states are visible to the cluster
+            __syncthreads();
             const int m = rs.misc[2];
             reevals += m;
             for (int q = ct; q < m * P; q += cstride) {
@@ -1135,7 +1103,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
                         : tk;
             }
             for (int q = ct; q < m; q += cstride) r.tab_bad[ls + rs.list[q]] = 0;
-            cluster_barrier();   // re-proposals visible
+            __syncthreads();
             const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
             for (int q = wid; q < m; q += nw) {
                 const int k = rs.list[q];
@@ -1164,10 +1132,10 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
                     if (rs.lps[rs.list[q]] > -INFINITY) rs.list[e++] = rs.list[q];
                 rs.misc[3] = e;
             }
-            cluster_barrier();   // tables visible
+            __syncthreads();
             PH_ADD(c_rep);
             PH_T0();
-            eval_slots_cluster(r, l, rs.list, rs.misc[3], sm, mixed, rs.part, rs.lls, 0, lead);
+            eval_direct(r, l, rs.list, rs.misc[3], sm, mixed, rs.lls, 0);
             PH_ADD(c_ev);
         }
     } else {
@@ -1238,7 +1206,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
                     r.th_s[(ls + C + w) * P + j] = v;
                 }
                 for (int w = ct; w < nv; w += cstride) r.tab_bad[ls + C + w] = 0;
-                cluster_barrier();   // variants visible
+                __syncthreads();
                 const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
                 for (int w = wid; w < nv; w += nw) {
                     const double lp = warp_prior(r, r.th_s + (ls + C + w) * P, rs.pa[rs.vs[w]]);
@@ -1261,12 +1229,12 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
                         if (rs.vlp[w] > -INFINITY) rs.list[e++] = C + w;
                     rs.misc[3] = e;
                 }
-                cluster_barrier();   // tables visible
+                __syncthreads();
                 const int ne = rs.misc[3];
                 variants += ne;
                 PH_ADD(c_rep);
                 PH_T0();
-                if (ne) eval_slots_cluster(r, l, rs.list, ne, sm, mixed, rs.part, rs.vll, C, lead);
+                if (ne) eval_direct(r, l, rs.list, ne, sm, mixed, rs.vll, C);
             }
             PH_ADD(c_ev);
             PH_T0();
@@ -1298,7 +1266,7 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
             __syncthreads();
             decided = rs.misc[0];
             write_accepts(r, l, type, n, rs, rs.misc[1], lead);
-            if (decided < n) cluster_barrier();   // the lead's accepted states are visible
+            __syncthreads();
             PH_ADD(c_dec);
         }
     }
@@ -1314,6 +1282,22 @@ k_sub_resolve(RunDev r, int pass, int level_begin, const int32_t *order)
         atomicAdd(&r.stats[ST_VARIANTS], (unsigned long long)variants);
         atomicAdd(&r.stats[ST_ROUNDS], (unsigned long long)rounds);
     }
+}
+
+
+// k_sub_resolve: one CTA per level of [level_begin, level_begin + n_level),
+// block q taking level order[q] (largest first; nullptr: index order), so
+// the longest levels start in the first wave.
+__global__ void __launch_bounds__(kResolveThreads, GGDMC_RESOLVE_MINB)
+k_sub_resolve(RunDev r, int level_begin, int n_level, const int32_t *order)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int q = blockIdx.x;
+    if (q >= n_level) return;
+    SubSmem sm = carve(smem_raw, r.m);
+    load_design(r, sm);
+    __syncthreads();
+    resolve_level(r, level_begin + (order ? order[q] : q), sm, smem_raw);
 }
 
 // ------------------------------------------------------------ phi level
@@ -1947,11 +1931,11 @@ cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
                                cudaStream_t st)
 {
+    (void)pass;
     // every subject at once runs largest first; a single subject keeps its index
     const int32_t *order = (level_count == r.S) ? r.sub_order : nullptr;
-    k_sub_resolve<<<level_count * kResolveCluster, kResolveThreads,
-                    sub_smem_bytes(r.m) + res_smem_bytes(r.C) + jit_stage_bytes(r.C, r.P), st>>>(
-        r, pass, level_begin, order);
+    const size_t smem = sub_smem_bytes(r.m) + res_smem_bytes(r.C) + jit_stage_bytes(r.C, r.P);
+    k_sub_resolve<<<level_count, kResolveThreads, smem, st>>>(r, level_begin, level_count, order);
     return cudaGetLastError();
 }
 
