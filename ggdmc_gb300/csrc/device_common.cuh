@@ -161,6 +161,46 @@ __device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int 
     return true;
 }
 
+// lba_logdens32 for a fixed accumulator count, with the cell's entry ids in
+// registers, winner first (the host stores each cell's entries that way).
+template <int K>
+__device__ __forceinline__ bool lba_logdens32_k(float t, const int (&ent)[K], const float4 *e32a,
+                                                const float2 *e32b, float &ld)
+{
+    if (!(t > 1e-4f)) return false;
+    const float it = __frcp_rn(t);
+    float pdf;
+    {
+        const float4 a = e32a[ent[0]];
+        const float2 b = e32b[ent[0]];
+        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
+        const float pz = phi32(cz), pm = phi32(czm);
+        const float sg = (czm >= 0.f) ? -1.f : 1.f;
+        const float d = sg * (ncdf32(sg * cz, pz) - ncdf32(sg * czm, pm));
+        pdf = fmaf(b.x, d, a.w * (pm - pz));
+    }
+    float surv = 1.f;
+    bool bad = false;
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        const float4 a = e32a[ent[k]];
+        const float2 b = e32b[ent[k]];
+        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
+        const float pz = phi32(cz), pm = phi32(czm);
+        const bool late = cz < 0.f;
+        const float sg = late ? 1.f : -1.f;
+        const float br = fmaf(cz, ncdf32(sg * cz, pz), -czm * ncdf32(sg * czm, pm)) + sg * (pz - pm);
+        const float tcs = t * a.w;
+        const float S = late ? fmaf(tcs, br, -b.y) : fmaf(-tcs, br, 1.f);
+        surv *= S;
+        bad |= late ? !(S >= 1e-9f && S * 32.f >= b.y) : !(S >= 1e-2f);
+    }
+    const float d = pdf * surv;
+    if (bad || !(pdf >= 1e-8f) || !(d > 0.f) || !(d < 3.0e38f)) return false;
+    ld = __logf(d);
+    return true;
+}
+
 // ------------------------------------------------------ DDM trial
 // Navarro & Fuss (2009) first-passage density of the Wiener process at the
 // lower boundary, with the series length chosen from its error bounds;

@@ -320,15 +320,18 @@ ggdmc_status build_design(ggdmc_handle *h, const ggdmc_model *m)
     std::vector<int32_t> t0s;
     for (int c = 0; c < m->n_cell; ++c) {
         if (m->resp[c] < 0 || m->resp[c] >= K) return fail(GGDMC_ERR_ARG, "resp index out of range");
-        cw[c] = (uint8_t)m->resp[c];
-        for (int k = 0; k < K; ++k) {
+        // entries winner first, then the other accumulators in order (the
+        // order of the survivor product is kept)
+        cw[c] = 0;
+        for (int kk = 0; kk < K; ++kk) {
+            const int k = (kk == 0) ? m->resp[c] : (kk <= m->resp[c] ? kk - 1 : kk);
             const int32_t *q = m->param_src + ((size_t)c * K + k) * NK;
             for (int j = 0; j < NK; ++j)
                 if (!check_src(q[j])) return fail(GGDMC_ERR_ARG, "parameter source out of range");
             double st0;
             if (!value_if_const(q[5], st0) || st0 != 0.0)
                 return fail(GGDMC_ERR_ARG, "LBA with st0 other than the constant 0 is not supported");
-            if (k == 0) ct0[c] = q[4];
+            if (kk == 0) ct0[c] = q[4];
             else if (q[4] != ct0[c])
                 return fail(GGDMC_ERR_ARG, "t0 must be the same for every accumulator of a cell");
             auto key = std::make_tuple(q[0], q[1], q[2], q[3]);
@@ -342,7 +345,7 @@ ggdmc_status build_design(ggdmc_handle *h, const ggdmc_model *m)
             } else {
                 id = it->second;
             }
-            cent[(size_t)c * K + k] = (uint8_t)id;
+            cent[(size_t)c * K + kk] = (uint8_t)id;
         }
     }
     for (int c = 0; c < m->n_cell; ++c) {

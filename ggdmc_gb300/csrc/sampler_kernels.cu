@@ -33,6 +33,11 @@
 #ifndef GGDMC_RESOLVE_MINB
 #define GGDMC_RESOLVE_MINB 1
 #endif
+// likelihood kernels: 6 blocks of 128 threads per SM (80 registers), which
+// measured faster than 4 (128 registers) or 1
+#ifndef GGDMC_LIK_MINB
+#define GGDMC_LIK_MINB 6
+#endif
 
 namespace ggdmc {
 
@@ -525,6 +530,40 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
     for (int g = 0; g < ng; ++g) out[g] = block_sum(acc[g] + ((double)ks[g] - (double)kc[g]), sm.red);
 }
 
+// The FP32 pass of group_loglik over trials [base, base + n) for K
+// accumulators: each trial's entry ids are read once and shared by the
+// group's proposals.
+template <int K>
+__device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, int n, const SubSmem &sm,
+                                                 const bool (&ok)[kGroup], float (&ks)[kGroup],
+                                                 float (&kc)[kGroup], int (&nfb)[kGroup])
+{
+    const int NE = r.m.n_ent, NT = r.m.n_t0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = r.cell[base + i];
+        const float2 rt = r.rt32[base + i];
+        int ent[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
+        const int q0 = sm.ct0[c];
+#pragma unroll
+        for (int g = 0; g < kGroup; ++g) {
+            if (!ok[g]) continue;
+            const float2 t0 = sm.t032[g * NT + q0];
+            const float t = (rt.x - t0.x) + (rt.y - t0.y);
+            float ld;
+            if (lba_logdens32_k<K>(t, ent, sm.e32a + g * NE, sm.e32b + g * NE, ld)) {
+                const float y = ld - kc[g];     // Kahan-compensated FP32 sum
+                const float tt = ks[g] + y;
+                kc[g] = (tt - ks[g]) - y;
+                ks[g] = tt;
+            } else {
+                ++nfb[g];
+            }
+        }
+    }
+}
+
 __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed,
                              double *out)
 {
@@ -555,24 +594,30 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
         ok[g] = g < ng && sm.flag[g] == 0;
         ks[g] = 0.f; kc[g] = 0.f; nfb[g] = 0;
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int c = r.cell[base + i];
-        const float2 rt = r.rt32[base + i];
-        const uint8_t *ents = sm.cent + c * K;
-        const int w = sm.cw[c], q0 = sm.ct0[c];
+    switch (K) {
+    case 2: lba_group_loop32<2>(r, base, n, sm, ok, ks, kc, nfb); break;
+    case 3: lba_group_loop32<3>(r, base, n, sm, ok, ks, kc, nfb); break;
+    case 4: lba_group_loop32<4>(r, base, n, sm, ok, ks, kc, nfb); break;
+    default:
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int c = r.cell[base + i];
+            const float2 rt = r.rt32[base + i];
+            const uint8_t *ents = sm.cent + c * K;
+            const int w = sm.cw[c], q0 = sm.ct0[c];
 #pragma unroll
-        for (int g = 0; g < kGroup; ++g) {
-            if (!ok[g]) continue;
-            const float2 t0 = sm.t032[g * NT + q0];
-            const float t = (rt.x - t0.x) + (rt.y - t0.y);
-            float ld;
-            if (lba_logdens32(t, ents, K, w, sm.e32a + g * NE, sm.e32b + g * NE, ld)) {
-                const float y = ld - kc[g];     // Kahan-compensated FP32 sum
-                const float tt = ks[g] + y;
-                kc[g] = (tt - ks[g]) - y;
-                ks[g] = tt;
-            } else {
-                ++nfb[g];
+            for (int g = 0; g < kGroup; ++g) {
+                if (!ok[g]) continue;
+                const float2 t0 = sm.t032[g * NT + q0];
+                const float t = (rt.x - t0.x) + (rt.y - t0.y);
+                float ld;
+                if (lba_logdens32(t, ents, K, w, sm.e32a + g * NE, sm.e32b + g * NE, ld)) {
+                    const float y = ld - kc[g];     // Kahan-compensated FP32 sum
+                    const float tt = ks[g] + y;
+                    kc[g] = (tt - ks[g]) - y;
+                    ks[g] = tt;
+                } else {
+                    ++nfb[g];
+                }
             }
         }
     }
@@ -861,7 +906,7 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_prior(RunDev r)
     }
 }
 
-__global__ void __launch_bounds__(kLikThreads) k_sub_loglik(RunDev r, const int32_t *items, int group)
+__global__ void __launch_bounds__(kLikThreads, GGDMC_LIK_MINB) k_sub_loglik(RunDev r, const int32_t *items, int group)
 {
     extern __shared__ __align__(16) char smem_raw[];
     __shared__ int s_slots[kGroup];
@@ -1805,7 +1850,7 @@ __global__ void k_next_iter(RunDev r)
 
 // ------------------------------------------------- batch likelihood API
 // theta [S][n_theta][P] -> out [S][n_theta]; grid = S * n_theta.
-__global__ void __launch_bounds__(kLikThreads) k_loglik_batch(RunDev r, const double *theta,
+__global__ void __launch_bounds__(kLikThreads, GGDMC_LIK_MINB) k_loglik_batch(RunDev r, const double *theta,
                                                               int n_theta, double *out)
 {
     extern __shared__ __align__(16) char smem_raw[];
