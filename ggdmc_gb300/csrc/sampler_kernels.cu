@@ -960,19 +960,103 @@ struct ResSmem {
     int *pa, *pb;           // [C] partners (crossover) / pa = subset (migration)
     int *acc, *accslot;     // [C] accepted steps of a scan and the slot they used
     int *list;              // [C + kVariants] steps / slots to evaluate
-    int16_t *ver;           // [C]
-    uint8_t *mod, *flag, *dec;   // [C]
     int *misc;              // 8
-    double *part;           // [C + kVariants] this CTA's partial sums of one evaluation
     int *vr, *vs;           // [kVariants] migration variant w: last rejected step (-1: none
                             // since the round began) and the step it serves
+    int *warp;              // [33] per-warp counts of a block compaction
+    int16_t *ver;           // [C]
+    uint8_t *mod, *dec;     // [C] step outcome in the sweep, Metropolis outcome of its proposal
+    uint8_t *cdec;          // [C] migration: outcome of the cascade value of step s
+    uint8_t *vdec;          // [kVariants] migration: outcome of variant w
 };
 
+__host__ __device__ inline size_t res_layout(int C, size_t off[8])
+{
+    size_t o = 0;
+    off[0] = o; o += sizeof(double) * 8 * (size_t)C;                     // lp .. accu
+    off[1] = o; o += sizeof(int) * (4 * (size_t)C + C + kVariants + 8 + 2 * kVariants + 33);
+    off[2] = o; o += sizeof(int16_t) * (size_t)C;
+    off[3] = o; o += 3 * (size_t)C + kVariants;
+    return align_up(o, 16);
+}
 __host__ __device__ inline size_t res_smem_bytes(int C)
 {
-    return align_up((size_t)C * (8 * sizeof(double) + 5 * sizeof(int) + sizeof(int16_t) + 3) +
-                        kVariants * sizeof(int) + 8 * sizeof(int) + 64, 16) +
-           (size_t)(C + kVariants) * sizeof(double) + 2 * kVariants * sizeof(int);
+    size_t off[8];
+    return res_layout(C, off);
+}
+__device__ ResSmem carve_res(char *base, int C)
+{
+    size_t off[8];
+    res_layout(C, off);
+    ResSmem s;
+    s.lp = (double *)(base + off[0]);
+    s.ll = s.lp + C;
+    s.lps = s.ll + C;
+    s.lls = s.lps + C;
+    s.cur = s.lls + C;
+    s.accu = s.cur + C;
+    s.vlp = s.accu + C;
+    s.vll = s.vlp + C;
+    s.pa = (int *)(base + off[1]);
+    s.pb = s.pa + C;
+    s.acc = s.pb + C;
+    s.accslot = s.acc + C;
+    s.list = s.accslot + C;
+    s.misc = s.list + C + kVariants;
+    s.vr = s.misc + 8;
+    s.vs = s.vr + kVariants;
+    s.warp = s.vs + kVariants;
+    s.ver = (int16_t *)(base + off[2]);
+    s.mod = (uint8_t *)(base + off[3]);
+    s.dec = s.mod + C;
+    s.cdec = s.dec + C;
+    s.vdec = s.cdec + C;
+    return s;
+}
+
+// Smallest i in [lo, hi) with pred(i), else hi.  All threads; every thread
+// gets the result.
+template <class F>
+__device__ __forceinline__ int block_first(int lo, int hi, F pred, int *tmp)
+{
+    if (threadIdx.x == 0) *tmp = hi;
+    __syncthreads();
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
+        if (pred(i)) atomicMin(tmp, i);
+    __syncthreads();
+    const int r = *tmp;
+    __syncthreads();
+    return r;
+}
+
+// The i in [lo, hi) with pred(i), ascending, into out; returns their count.
+// All threads (blockDim.x a multiple of 32, at most 1024).
+template <class F>
+__device__ __forceinline__ int block_compact(int lo, int hi, F pred, int *out, int *warp)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int total = 0;
+    for (int b0 = lo; b0 < hi; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const bool p = i < hi && pred(i);
+        const unsigned m = __ballot_sync(0xffffffffu, p);
+        if (lane == 0) warp[wid] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int w = 0; w < nw; ++w) {
+                const int c = warp[w];
+                warp[w] = acc;
+                acc += c;
+            }
+            warp[32] = acc;
+        }
+        __syncthreads();
+        if (p) out[total + warp[wid] + __popc(m & ((1u << lane) - 1u))] = i;
+        total += warp[32];
+        __syncthreads();
+    }
+    return total;
 }
 
 // The subject's jitter rows are staged in shared memory when they fit.
@@ -983,33 +1067,6 @@ __host__ __device__ inline size_t jit_stage_bytes(int C, int P)
     return b <= kJitStage ? b : 0;
 }
 
-__device__ ResSmem carve_res(char *base, int C)
-{
-    ResSmem s;
-    s.lp = (double *)base;
-    s.ll = s.lp + C;
-    s.lps = s.ll + C;
-    s.lls = s.lps + C;
-    s.cur = s.lls + C;
-    s.accu = s.cur + C;
-    s.vlp = s.accu + C;
-    s.vll = s.vlp + C;
-    s.pa = (int *)(s.vll + C);
-    s.pb = s.pa + C;
-    s.acc = s.pb + C;
-    s.accslot = s.acc + C;
-    s.list = s.accslot + C;
-    s.misc = s.list + C + kVariants;
-    s.ver = (int16_t *)(s.misc + 8);
-    s.mod = (uint8_t *)(s.ver + C);
-    s.flag = s.mod + C;
-    s.dec = s.flag + C;
-    s.part = (double *)(base + align_up((size_t)C * (8 * sizeof(double) + 5 * sizeof(int) + sizeof(int16_t) + 3) +
-                                            kVariants * sizeof(int) + 8 * sizeof(int) + 64, 16));
-    s.vr = (int *)(s.part + C + kVariants);
-    s.vs = s.vr + kVariants;
-    return s;
-}
 
 // Copy the rows of the steps accepted by the last scan into the state.
 __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na, bool lead)
@@ -1105,38 +1162,32 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             for (int k = decided + threadIdx.x; k < n; k += blockDim.x)
                 rs.dec[k] = mh_accept((rs.lps[k] + rs.lls[k]) - (rs.ll[k] + rs.lp[k]), rs.accu[k]) ? 1 : 0;
             __syncthreads();
-            if (threadIdx.x == 0) {
-                int i = decided, na = 0;
-                while (i < n) {
-                    const int a = rs.pa[i], b = rs.pb[i], v = rs.ver[i];
-                    if ((a >= v && a < i && rs.mod[a]) || (b >= v && b < i && rs.mod[b])) break;
-                    rs.mod[i] = rs.dec[i];
-                    if (rs.dec[i]) { rs.acc[na] = i; rs.accslot[na] = i; ++na; }
-                    ++i;
-                }
-                rs.misc[0] = i;
-                rs.misc[1] = na;
-            }
+            // The decided prefix ends at the first step one of whose partners
+            // moved after that step's proposal was made: a partner accepted in
+            // an earlier round (mod) or earlier in this one (dec).
+            const int dc = decided;
+            const int d = block_first(dc, n, [&](int i) {
+                const int a = rs.pa[i], b = rs.pb[i], v = rs.ver[i];
+                const bool ma = a >= v && a < i && (a < dc ? rs.mod[a] : rs.dec[a]);
+                const bool mb = b >= v && b < i && (b < dc ? rs.mod[b] : rs.dec[b]);
+                return ma || mb;
+            }, rs.misc + 6);
+            for (int i = dc + threadIdx.x; i < d; i += blockDim.x) rs.mod[i] = rs.dec[i];
+            const int na = block_compact(dc, d, [&](int i) { return rs.dec[i] != 0; }, rs.acc, rs.warp);
+            for (int q = threadIdx.x; q < na; q += blockDim.x) rs.accslot[q] = rs.acc[q];
             __syncthreads();
-            const int d = rs.misc[0];
-            write_accepts(r, l, type, n, rs, rs.misc[1], lead);
+            write_accepts(r, l, type, n, rs, na, lead);
             decided = d;
             PH_ADD(c_dec);
             if (decided >= n) break;
             PH_T0();
             // stale chains: a partner in [ver, decided) moved
-            if (threadIdx.x == 0) {
-                int m = 0;
-                for (int k = decided; k < n; ++k) {
-                    const int a = rs.pa[k], b = rs.pb[k], v = rs.ver[k];
-                    if ((a >= v && a < decided && rs.mod[a]) || (b >= v && b < decided && rs.mod[b]))
-                        rs.list[m++] = k;
-                    rs.ver[k] = (int16_t)decided;
-                }
-                rs.misc[2] = m;
-            }
+            const int m = block_compact(decided, n, [&](int k) {
+                const int a = rs.pa[k], b = rs.pb[k], v = rs.ver[k];
+                return (a >= v && a < decided && rs.mod[a]) || (b >= v && b < decided && rs.mod[b]);
+            }, rs.list, rs.warp);
+            for (int k = decided + threadIdx.x; k < n; k += blockDim.x) rs.ver[k] = (int16_t)decided;
             __syncthreads();
-            const int m = rs.misc[2];
             reevals += m;
             for (int q = ct; q < m * P; q += cstride) {
                 const int k = rs.list[q / P], j = q % P;
@@ -1171,16 +1222,13 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             }
             __syncthreads();
             // evaluate the re-proposed chains whose prior is finite
-            if (threadIdx.x == 0) {
-                int e = 0;
-                for (int q = 0; q < m; ++q)
-                    if (rs.lps[rs.list[q]] > -INFINITY) rs.list[e++] = rs.list[q];
-                rs.misc[3] = e;
-            }
+            const int e = block_compact(0, m, [&](int q) { return rs.lps[rs.list[q]] > -INFINITY; },
+                                        rs.acc, rs.warp);
+            for (int q = threadIdx.x; q < e; q += blockDim.x) rs.list[q] = rs.list[rs.acc[q]];
             __syncthreads();
             PH_ADD(c_rep);
             PH_T0();
-            eval_direct(r, l, rs.list, rs.misc[3], sm, mixed, rs.lls, 0);
+            eval_direct(r, l, rs.list, e, sm, mixed, rs.lls, 0);
             PH_ADD(c_ev);
         }
     } else {
@@ -1196,7 +1244,14 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             rs.vll[w] = r.ll_s[ls + C + w];
         }
         __syncthreads();
-        int mig_acc = 0;   // accepted steps so far (thread 0's count)
+        // Metropolis outcomes of every step's start-of-pass proposal and of
+        // its cascade value (draw-free: the accept uniforms are fixed)
+        for (int s = threadIdx.x; s < n; s += blockDim.x) {
+            rs.dec[s] = mh_accept((rs.lps[s] + rs.lls[s]) - rs.cur[s], rs.accu[s]) ? 1 : 0;
+            rs.cdec[s] = (s > 0 && mh_accept((rs.vlp[s] + rs.vll[s]) - rs.cur[s], rs.accu[s])) ? 1 : 0;
+        }
+        if (threadIdx.x == 0) rs.misc[5] = 0;   // accepted steps so far
+        __syncthreads();
         while (decided < n) {
             ++rounds;
             PH_T0();
@@ -1208,37 +1263,47 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             // new source plus the jitters of d..s.  Evaluate the kMigRound
             // most likely of these, scored with this pass's acceptance so far.
             if (d > 0) {
-                if (threadIdx.x == 0) {
-                    const double a = (mig_acc + 1.0) / (d + 2.0);
-                    double best[kMigRound] = {};
-                    int nv = 0;
-                    auto offer = [&](double sc, int vr, int vs) {
-                        int pos = nv;
-                        while (pos > 0 && best[pos - 1] < sc) --pos;
-                        if (pos >= kMigRound) return;
-                        const int last = (nv < kMigRound) ? nv : kMigRound - 1;
-                        for (int q = last; q > pos; --q) {
-                            best[q] = best[q - 1];
-                            rs.vr[q] = rs.vr[q - 1];
-                            rs.vs[q] = rs.vs[q - 1];
+                if (threadIdx.x < 32) {
+                    // candidate c < kVariants: the run value for step d + c
+                    // (score a^c, 2 for c = 0); c >= kVariants: the value for
+                    // step rj + 1 + k after a reject at rj = d + (c - kVariants) / 3,
+                    // k = 1 + (c - kVariants) % 3 (score (1 - a) a^k 0.95^(rj - d));
+                    // the kMigRound best, ties to the lower c
+                    const int c = threadIdx.x;
+                    const double a = (rs.misc[5] + 1.0) / (d + 2.0);
+                    double sc = -1.0;
+                    int vr = 0, vs = 0;
+                    if (c < kVariants) {
+                        if (d + c < n) {
+                            double ak = 1.0;
+                            for (int k = 0; k < c; ++k) ak *= a;
+                            sc = (c == 0) ? 2.0 : ak;
+                            vr = -1;
+                            vs = d + c;
                         }
-                        best[pos] = sc;
-                        rs.vr[pos] = vr;
-                        rs.vs[pos] = vs;
-                        if (nv < kMigRound) ++nv;
-                    };
-                    double ak = 1.0;
-                    for (int k = 0; k < kVariants && d + k < n; ++k, ak *= a)
-                        offer(k == 0 ? 2.0 : ak, -1, d + k);
-                    double reach = 1.0;
-                    for (int rj = d; rj < d + kVariants && rj < n; ++rj, reach *= 0.95) {
-                        double sc = (1.0 - a) * reach;
-                        for (int k = 1; k <= 3 && rj + 1 + k < n; ++k) {
-                            sc *= a;
-                            offer(sc, rj, rj + 1 + k);
+                    } else {
+                        const int rj = d + (c - kVariants) / 3, k = 1 + (c - kVariants) % 3;
+                        if (rj + 1 + k < n) {
+                            double v = 1.0 - a;
+                            for (int q = 0; q < k; ++q) v *= a;
+                            for (int q = d; q < rj; ++q) v *= 0.95;
+                            sc = v;
+                            vr = rj;
+                            vs = rj + 1 + k;
                         }
                     }
-                    rs.misc[4] = nv;
+                    int rank = 0;
+                    for (int o = 0; o < 32; ++o) {
+                        const double so = __shfl_sync(0xffffffffu, sc, o);
+                        rank += (so > sc || (so == sc && o < c)) ? 1 : 0;
+                    }
+                    const bool valid = sc > 0.0;
+                    if (valid && rank < kMigRound) {
+                        rs.vr[rank] = vr;
+                        rs.vs[rank] = vs;
+                    }
+                    const int nvalid = __popc(__ballot_sync(0xffffffffu, valid));
+                    if (c == 0) rs.misc[4] = min(kMigRound, nvalid);
                 }
                 __syncthreads();
                 const int nv = rs.misc[4];
@@ -1280,33 +1345,47 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                 PH_ADD(c_rep);
                 PH_T0();
                 if (ne) eval_direct(r, l, rs.list, ne, sm, mixed, rs.vll, C);
+                for (int w = threadIdx.x; w < nv; w += blockDim.x)
+                    rs.vdec[w] = mh_accept((rs.vlp[w] + rs.vll[w]) - rs.cur[rs.vs[w]], rs.accu[rs.vs[w]]) ? 1 : 0;
+                __syncthreads();
             }
             PH_ADD(c_ev);
             PH_T0();
             if (threadIdx.x == 0) {
+                // the steps in order, each with the outcome of the value it
+                // needs, until one needs a value not evaluated yet
                 const int nv = (d == 0) ? n : rs.misc[4];
-                int s = d, na = 0, lastrej = -1;
+                int s = d, na = 0, lastrej = -1, nacc = rs.misc[5];
                 while (s < n) {
                     int slot = -1;
+                    bool ok = false;
                     if (s > 0 && !rs.mod[s - 1]) {
                         slot = s;                    // source unchanged: the spec proposal
+                        ok = rs.dec[s];
                     } else if (d == 0) {
-                        slot = (s == 0) ? 0 : (lastrej < 0 ? C + s : -1);   // cascade from step 0
+                        if (s == 0) {
+                            slot = 0;
+                            ok = rs.dec[0];
+                        } else if (lastrej < 0) {    // cascade from step 0
+                            slot = C + s;
+                            ok = rs.cdec[s];
+                        }
                     } else {
                         for (int w = 0; w < nv; ++w)
-                            if (rs.vs[w] == s && rs.vr[w] == lastrej) slot = C + w;
+                            if (rs.vs[w] == s && rs.vr[w] == lastrej) {
+                                slot = C + w;
+                                ok = rs.vdec[w];
+                            }
                     }
                     if (slot < 0) break;
-                    const double lpv = (slot < C) ? rs.lps[slot] : rs.vlp[slot - C];
-                    const double llv = (slot < C) ? rs.lls[slot] : rs.vll[slot - C];
-                    const bool ok = mh_accept((lpv + llv) - rs.cur[s], rs.accu[s]);
                     rs.mod[s] = ok ? 1 : 0;
-                    if (ok) { rs.acc[na] = s; rs.accslot[na] = slot; ++na; ++mig_acc; }
+                    if (ok) { rs.acc[na] = s; rs.accslot[na] = slot; ++na; ++nacc; }
                     else lastrej = s;
                     ++s;
                 }
                 rs.misc[0] = s;
                 rs.misc[1] = na;
+                rs.misc[5] = nacc;
             }
             __syncthreads();
             decided = rs.misc[0];
