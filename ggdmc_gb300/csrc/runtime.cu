@@ -639,8 +639,9 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         cudaError_t e;
         // Hierarchical and batched: the first subject pass's proposals and
         // their speculative evaluation read nothing the phi level writes
-        // (only their priors do), so they run on a second stream beside it;
-        // k_sub_prior scores the priors after the join.
+        // (only their priors do), so they run on a second stream beside it,
+        // at low priority so the phi level's small kernels get SMs first;
+        // k_sub_resolve scores the priors after the join.
         const bool fork = hier && S > 0 && Pphi > 0 && !plain;
         if (fork) {
             if ((e = cudaEventRecord(h->ev_fork, st))) return e;
@@ -670,9 +671,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             for (int p = 0; p < npass; ++p) {
                 if (fork && p == 0) {
                     if ((e = cudaStreamWaitEvent(st, h->ev_join, 0))) return e;
-                    if ((e = launch_sub_prior(r, st))) return e;
-                    if ((e = launch_sub_resolve(r, 0, 0, S, st))) return e;
-                    launches_per_iter += 2;
+                    if ((e = launch_sub_resolve(r, 0, 0, S, true, st))) return e;
+                    ++launches_per_iter;
                     continue;
                 }
                 if ((e = launch_sub_propose(r, p, false, st))) return e;
@@ -680,12 +680,12 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
                 if (plain) {
                     for (int l = 0; l < S; ++l) {
                         if ((e = launch_sub_loglik(r, h->items_plain.p + (size_t)l * CS, CS, 1, st))) return e;
-                        if ((e = launch_sub_resolve(r, p, l, 1, st))) return e;
+                        if ((e = launch_sub_resolve(r, p, l, 1, false, st))) return e;
                         launches_per_iter += 2;
                     }
                 } else {
                     if ((e = launch_sub_loglik(r, h->items.p, n_spec_items, spec_group, st))) return e;
-                    if ((e = launch_sub_resolve(r, p, 0, S, st))) return e;
+                    if ((e = launch_sub_resolve(r, p, 0, S, false, st))) return e;
                     launches_per_iter += 2;
                 }
             }
@@ -735,7 +735,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             return fail(GGDMC_ERR_CUDA, std::string("graph capture: ") +
                                             cudaGetErrorString(ce ? ce : ee));
         }
-        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaError_t ie = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
         if (ie) {
             cleanup_events();
             cudaGraphDestroy(graph);
@@ -879,8 +879,10 @@ ggdmc_status make_handle(const ggdmc_model *model, const ggdmc_data *data, ggdmc
     cudaGetDevice(&h->device);
     cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
     if (h->n_sm < 1) h->n_sm = 1;
-    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (!e) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+    int prio_low = 0, prio_high = 0;
+    e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (!e) e = cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_high);
+    if (!e) e = cudaStreamCreateWithPriority(&h->stream2, cudaStreamNonBlocking, prio_low);
     if (!e) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
     ggdmc_status s = e ? fail(GGDMC_ERR_CUDA, std::string("stream / event create: ") + cudaGetErrorString(e))

@@ -105,11 +105,10 @@ struct RunDev {
 // --------------------------------------------------------------- launchers
 // (defined in sampler_kernels.cu)
 cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, cudaStream_t st);
-cudaError_t launch_sub_prior(const RunDev &r, cudaStream_t st);
 cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, int group,
                               cudaStream_t st);
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
-                               cudaStream_t st);
+                               bool score_priors, cudaStream_t st);
 cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st);
 cudaError_t launch_phi_propose(const RunDev &r, int pass, cudaStream_t st);
 cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st);

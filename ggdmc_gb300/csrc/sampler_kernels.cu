@@ -257,7 +257,10 @@ __device__ __forceinline__ void partners(const RunDev &r, int64_t it, int lev, i
 
 // get_subchains (src/de.cpp:62-78) from uniforms u[1..C+1] drawn in
 // parallel; single thread.
-__device__ int subchains_from(int C, const double *u, int *sub, int *perm)
+// Migration subset (src/de.cpp:62-78): n = ceil(C u1) clamped to [2, C]
+// chains picked by a partial Fisher-Yates shuffle on the keyed uniforms
+// (perm[0..n) after the call); subchains_sort then sorts them ascending.
+__device__ int subchains_pick(int C, const double *u, int *perm)
 {
     int n = (int)ceil((double)C * u[1]);
     if (n < 2) n = 2;
@@ -268,14 +271,20 @@ __device__ int subchains_from(int C, const double *u, int *sub, int *perm)
         if (q > C - 1) q = C - 1;
         const int t = perm[j]; perm[j] = perm[q]; perm[q] = t;
     }
-    for (int j = 0; j < n; ++j) sub[j] = perm[j];
-    for (int j = 1; j < n; ++j) {
-        const int x = sub[j];
-        int q = j - 1;
-        while (q >= 0 && sub[q] > x) { sub[q + 1] = sub[q]; --q; }
-        sub[q + 1] = x;
-    }
     return n;
+}
+
+// sub = perm[0..n) in ascending order (the picks are distinct: each one's
+// rank is the number of smaller picks).  All threads.
+__device__ __forceinline__ void subchains_sort(const int *perm, int n, int *sub)
+{
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const int x = perm[j];
+        int rank = 0;
+        for (int i = 0; i < n; ++i) rank += (perm[i] < x) ? 1 : 0;
+        sub[rank] = x;
+    }
+    __syncthreads();
 }
 
 // one component of a crossover proposal (src/de.cpp:111-142):
@@ -716,8 +725,8 @@ __device__ __forceinline__ double warp_prior(const RunDev &r, const double *th, 
 // grid = S.
 // In a hierarchical sweep the subject proposals are built while the phi
 // level runs (defer_prior): the prior, the only term that reads phi, is
-// scored after both by k_sub_prior, and a proposal is evaluated when it lies
-// in the prior's support, which does not depend on phi.
+// scored after both, at the start of k_sub_resolve, and a proposal is
+// evaluated when it lies in the prior's support, which does not depend on phi.
 __device__ __forceinline__ bool in_support(const RunDev &r, const double *th)
 {
     for (int j = 0; j < r.P; ++j)
@@ -760,9 +769,11 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
         for (int q = 1 + threadIdx.x; q < C + 2; q += blockDim.x) s_u[q] = uniform(r.ds, it, lev, pass, q);
         __syncthreads();
         if (threadIdx.x == 0) {
-            s_n = subchains_from(C, s_u, s_sub, s_perm);
+            s_n = subchains_pick(C, s_u, s_perm);
             atomicAdd(&r.stats[ST_MIGRATIONS], 1ull);
         }
+        __syncthreads();
+        subchains_sort(s_perm, s_n, s_sub);
     } else if (threadIdx.x == 0) {
         s_n = (type == PASS_SKIP) ? 0 : C;
     }
@@ -886,26 +897,6 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
 // k_sub_loglik: the hot kernel.  One CTA per work item = up to kGroup
 // proposals of one subject, items in descending trial-count order (longest
 // first keeps the tail short).  item = level * CS + first slot.
-// k_sub_prior: the deferred priors of a pass's proposals (and of the
-// migration cascade), a warp per slot, with the phi chains of this sweep.
-__global__ void __launch_bounds__(kProposeThreads) k_sub_prior(RunDev r)
-{
-    const int l = blockIdx.x;
-    const int type = r.ptype[l], n = r.nstep[l];
-    if (type == PASS_SKIP || n == 0) return;
-    const int C = r.C, P = r.P, CS = r.CS;
-    const double *ths = r.th_s + (size_t)l * CS * P;
-    const int nv = (type == PASS_MIG) ? n : 0;
-    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int q = wid; q < n + nv; q += nw) {
-        const int slot = (q < n) ? q : C + (q - n);
-        const int k = (q < n) ? q : q - n;
-        const int owner = (type == PASS_CROSS) ? k : r.sub[(size_t)l * C + k];
-        const double lp = (slot == C) ? -INFINITY : warp_prior(r, ths + (size_t)slot * P, owner);
-        if ((threadIdx.x & 31) == 0) r.lp_s[(size_t)l * CS + slot] = lp;
-    }
-}
-
 __global__ void __launch_bounds__(kLikThreads, GGDMC_LIK_MINB) k_sub_loglik(RunDev r, const int32_t *items, int group)
 {
     extern __shared__ __align__(16) char smem_raw[];
@@ -1105,7 +1096,7 @@ __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &
 // (valid after a rejection) and the cascade from step 0 (valid while every
 // step accepts); later rounds evaluate the most likely values the next steps
 // can need.
-__device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_raw)
+__device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_raw, bool score_priors)
 {
     const bool lead = true;
     const int type = r.ptype[l];
@@ -1115,6 +1106,20 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
     const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
     const bool mixed = r.prec == PREC_MIXED;
     ResSmem rs = carve_res(smem_raw + sub_smem_bytes(r.m), C);
+    if (score_priors) {
+        // deferred priors of the pass's proposals (and migration cascade),
+        // with the phi chains of this sweep: a warp per slot
+        const int nv = (type == PASS_MIG) ? n : 0;
+        const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int q = wid; q < n + nv; q += nw) {
+            const int slot = (q < n) ? q : C + (q - n);
+            const int k = (q < n) ? q : q - n;
+            const int owner = (type == PASS_CROSS) ? k : r.sub[lc + k];
+            const double lp = (slot == C) ? -INFINITY : warp_prior(r, r.th_s + (ls + slot) * P, owner);
+            if ((threadIdx.x & 31) == 0) r.lp_s[ls + slot] = lp;
+        }
+        __syncthreads();
+    }
     for (int k = threadIdx.x; k < C; k += blockDim.x) {
         rs.lp[k] = r.lp[lc + k];
         rs.ll[k] = r.ll[lc + k];
@@ -1413,7 +1418,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
 // block q taking level order[q] (largest first; nullptr: index order), so
 // the longest levels start in the first wave.
 __global__ void __launch_bounds__(kResolveThreads, GGDMC_RESOLVE_MINB)
-k_sub_resolve(RunDev r, int level_begin, int n_level, const int32_t *order)
+k_sub_resolve(RunDev r, int level_begin, int n_level, const int32_t *order, int score_priors)
 {
     extern __shared__ __align__(16) char smem_raw[];
     const int q = blockIdx.x;
@@ -1421,7 +1426,7 @@ k_sub_resolve(RunDev r, int level_begin, int n_level, const int32_t *order)
     SubSmem sm = carve(smem_raw, r.m);
     load_design(r, sm);
     __syncthreads();
-    resolve_level(r, level_begin + (order ? order[q] : q), sm, smem_raw);
+    resolve_level(r, level_begin + (order ? order[q] : q), sm, smem_raw, score_priors != 0);
 }
 
 // ------------------------------------------------------------ phi level
@@ -1492,9 +1497,11 @@ __global__ void __launch_bounds__(kPhiProposeThreads) k_phi_propose(RunDev r, in
         for (int q = 1 + threadIdx.x; q < C + 2; q += blockDim.x) s_u[q] = uniform(r.ds, it, 0, pass, q);
         __syncthreads();
         if (threadIdx.x == 0) {
-            s_n = subchains_from(C, s_u, s_sub, s_perm);
+            s_n = subchains_pick(C, s_u, s_perm);
             atomicAdd(&r.stats[ST_MIGRATIONS], 1ull);
         }
+        __syncthreads();
+        subchains_sort(s_perm, s_n, s_sub);
     } else if (threadIdx.x == 0) {
         s_n = (type == PASS_SKIP) ? 0 : C;
     }
@@ -2039,11 +2046,6 @@ cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_sub_prior(const RunDev &r, cudaStream_t st)
-{
-    k_sub_prior<<<r.S, kProposeThreads, 0, st>>>(r);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, int group,
                               cudaStream_t st)
@@ -2053,13 +2055,14 @@ cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items
 }
 
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
-                               cudaStream_t st)
+                               bool score_priors, cudaStream_t st)
 {
     (void)pass;
     // every subject at once runs largest first; a single subject keeps its index
     const int32_t *order = (level_count == r.S) ? r.sub_order : nullptr;
     const size_t smem = sub_smem_bytes(r.m) + res_smem_bytes(r.C) + jit_stage_bytes(r.C, r.P);
-    k_sub_resolve<<<level_count, kResolveThreads, smem, st>>>(r, level_begin, level_count, order);
+    k_sub_resolve<<<level_count, kResolveThreads, smem, st>>>(r, level_begin, level_count, order,
+                                                             score_priors ? 1 : 0);
     return cudaGetLastError();
 }
 
