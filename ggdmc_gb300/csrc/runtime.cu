@@ -898,6 +898,61 @@ ggdmc_status make_handle(const ggdmc_model *model, const ggdmc_data *data, ggdmc
     return GGDMC_OK;
 }
 
+// Rejection draws of one level set (S levels x C chains of P parameters) until
+// every pair has a finite prior and likelihood; score() fills d_ll from
+// d_theta.  On return the host arrays hold theta, lp and ll.
+template <class Score>
+static ggdmc_status init_level(ggdmc_handle *h, const ggdmc_prior *prior, int S, int C, int P, int level0,
+                               int max_attempts, uint64_t seed, DevBuf<double> &d_theta, Score score,
+                               std::vector<double> &th, std::vector<double> &lp, std::vector<double> &ll)
+{
+    cudaStream_t st = h->stream;
+    std::vector<double> rows;
+    ggdmc_status s = prior_rows(prior, rows);
+    if (s) return s;
+    const size_t n = (size_t)S * C;
+    DevBuf<double> d_rows, d_lp, d_ll;
+    DevBuf<int32_t> d_att;
+    DevBuf<uint8_t> d_done;
+    CU(d_rows.upload(rows.data(), rows.size(), st));
+    CU(d_theta.alloc(n * P));
+    CU(d_lp.alloc(n));
+    CU(d_ll.alloc(n));
+    std::vector<int32_t> att(n, 0);
+    std::vector<uint8_t> done(n, 0);
+    lp.assign(n, 0.0);
+    ll.assign(n, 0.0);
+    size_t left = n;
+    for (int a = 0; a < max_attempts && left; ++a) {
+        CU(d_att.upload(att.data(), n, st));
+        CU(d_done.upload(done.data(), n, st));
+        CU(launch_init_draw(d_rows.p, P, C, level0, S, d_att.p, d_done.p, seed, d_theta.p, st));
+        CU(launch_logprior(d_rows.p, P, d_theta.p, (int)n, d_lp.p, st));
+        CU(score(d_theta.p, d_ll.p));
+        std::vector<double> lp_a(n), ll_a(n);
+        CU(cudaMemcpyAsync(lp_a.data(), d_lp.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(ll_a.data(), d_ll.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if ((s = wait_stream(st))) return s;
+        for (size_t i = 0; i < n; ++i) {
+            if (done[i]) continue;
+            if (std::isfinite(lp_a[i]) && std::isfinite(ll_a[i])) {
+                done[i] = 1;
+                lp[i] = lp_a[i];
+                ll[i] = ll_a[i];
+                --left;
+            } else {
+                ++att[i];
+            }
+        }
+    }
+    if (left)
+        return fail(GGDMC_ERR_NUMERIC, std::to_string(left) + " chain(s) found no start with a finite prior and "
+                                       "likelihood in " + std::to_string(max_attempts) + " attempts");
+    th.resize(n * P);
+    CU(cudaMemcpyAsync(th.data(), d_theta.p, sizeof(double) * n * P, cudaMemcpyDeviceToHost, st));
+    return wait_stream(st);
+}
+
 }  // namespace
 
 // ================================================================== C ABI
@@ -1047,6 +1102,56 @@ ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta,
     CU(launch_loglik_batch(r, h->io_a.p, n_theta, h->io_b.p, h->stream));
     CU(cudaMemcpyAsync(out, h->io_b.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, h->stream));
     return wait_stream(h->stream);
+}
+
+ggdmc_status ggdmc_initialise(ggdmc_handle *h, const ggdmc_prior *p_prior, const ggdmc_prior *h_prior,
+                              int32_t nchain, int32_t max_attempts, uint64_t seed, int32_t precision,
+                              ggdmc_chain_state *subj_state, ggdmc_chain_state *phi_state)
+{
+    if (!h || !p_prior || !subj_state || nchain < 1 || max_attempts < 1)
+        return fail(GGDMC_ERR_ARG, "bad initialise arguments");
+    if (h->S < 1) return fail(GGDMC_ERR_ARG, "handle has no subjects");
+    if (p_prior->n_par != h->n_par) return fail(GGDMC_ERR_ARG, "p_prior must have one row per parameter");
+    if (h_prior && (!phi_state || h_prior->n_par != 2 * h->n_par))
+        return fail(GGDMC_ERR_ARG, "h_prior needs 2 x n_par rows and a phi_state");
+    const int S = h->S, C = nchain, P = h->n_par;
+    const RunDev lr = loglik_desc(h, precision);
+    DevBuf<double> d_th;
+    std::vector<double> th, lp, ll;
+    ggdmc_status s = init_level(h, p_prior, S, C, P, 1, max_attempts, seed, d_th,
+                                [&](const double *t, double *o) { return launch_loglik_batch(lr, t, C, o, h->stream); },
+                                th, lp, ll);
+    if (s) return s;
+    for (int l = 0; l < S; ++l) {
+        const ggdmc_chain_state &cs = subj_state[l];
+        if (!cs.theta || !cs.lp || !cs.ll) return fail(GGDMC_ERR_ARG, "subject state incomplete");
+        std::memcpy(cs.theta, th.data() + (size_t)l * C * P, sizeof(double) * C * P);
+        std::memcpy(cs.lp, lp.data() + (size_t)l * C, sizeof(double) * C);
+        std::memcpy(cs.ll, ll.data() + (size_t)l * C, sizeof(double) * C);
+    }
+    if (!h_prior) return GGDMC_OK;
+    // phi: hyper log-likelihood against the subjects' chains c (src/de.cpp:245-270)
+    if (2 * P > kMaxTheta) return fail(GGDMC_ERR_ARG, "too many parameters");
+    std::vector<double> bounds(2 * (size_t)P);
+    for (int j = 0; j < P; ++j) {
+        bounds[2 * j] = p_prior->table[6 * j + 2];
+        bounds[2 * j + 1] = p_prior->table[6 * j + 3];
+    }
+    DevBuf<double> d_b, d_phi;
+    CU(d_b.upload(bounds.data(), bounds.size(), h->stream));
+    RunDev hr{};
+    hr.C = C; hr.P = P; hr.Pphi = 2 * P; hr.S = S;
+    hr.th = d_th.p; hr.pp_bounds = d_b.p;
+    hr.prec = (precision == GGDMC_MIXED) ? PREC_MIXED : PREC_FP64;
+    std::vector<double> pth, plp, pll;
+    s = init_level(h, h_prior, 1, C, 2 * P, 0, max_attempts, seed, d_phi,
+                   [&](const double *t, double *o) { return launch_loghlike(hr, t, o, h->stream); }, pth, plp, pll);
+    if (s) return s;
+    if (!phi_state->theta || !phi_state->lp || !phi_state->ll) return fail(GGDMC_ERR_ARG, "phi state incomplete");
+    std::memcpy(phi_state->theta, pth.data(), sizeof(double) * C * 2 * P);
+    std::memcpy(phi_state->lp, plp.data(), sizeof(double) * C);
+    std::memcpy(phi_state->ll, pll.data(), sizeof(double) * C);
+    return GGDMC_OK;
 }
 
 ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta, int32_t precision, double *out)

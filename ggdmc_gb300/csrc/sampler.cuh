@@ -119,6 +119,8 @@ cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_thet
                                 cudaStream_t st);
 cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *out,
                                  cudaStream_t st);
+cudaError_t launch_init_draw(const double *rows, int P, int C, int level0, int n_level, const int32_t *attempt,
+                             const uint8_t *done, uint64_t seed, double *theta, cudaStream_t st);
 cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
                             cudaStream_t st);
 cudaError_t launch_loghlike(const RunDev &r, const double *phi, double *out, cudaStream_t st);

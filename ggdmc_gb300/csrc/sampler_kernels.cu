@@ -2003,6 +2003,36 @@ __global__ void __launch_bounds__(kLikThreads) k_trial_logdens(RunDev r, const d
 }
 
 // sumlogprior of n vectors against fixed rows; one thread per vector.
+// Start-state draws (initialise_theta / initialise_phi, R/phi.R:141-332):
+// parameter j of chain c at level v0 + v is the prior's inverse distribution
+// function at the keyed uniform (iteration 0, level v0 + v, pass = the pair's
+// attempt, slot c * P + j), for the (level, chain) pairs not yet accepted.
+// rows: the device prior rows (id, p0, p1, lower, upper, constant).
+__device__ __forceinline__ double prior_draw(const double *row, double u)
+{
+    if ((int)row[0] != 1) return row[1] + u * (row[2] - row[1]);
+    const double mu = row[1], sg = row[2], lo = row[3], hi = row[4];
+    const double pa = isinf(lo) ? 0.0 : Phi64((lo - mu) / sg);
+    const double pb = isinf(hi) ? 1.0 : Phi64((hi - mu) / sg);
+    double x = mu + sg * normcdfinv(pa + u * (pb - pa));
+    if (x < lo) x = lo;
+    if (x > hi) x = hi;
+    return x;
+}
+
+__global__ void k_init_draw(const double *rows, int P, int C, int level0, int n_level,
+                            const int32_t *attempt, const uint8_t *done, uint64_t seed, double *theta)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n_level * C * P) return;
+    const int j = (int)(idx % P);
+    const int64_t lc = idx / P;
+    if (done[lc]) return;
+    const int c = (int)(lc % C), v = (int)(lc / C);
+    const DrawSrc ds{nullptr, seed, 1, 1, 1};
+    theta[idx] = prior_draw(rows + kPriorRow * j, uniform(ds, 0, level0 + v, attempt[lc], (int64_t)c * P + j));
+}
+
 __global__ void k_logprior(const double *rows, int P, const double *theta, int n, double *out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2112,6 +2142,15 @@ cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_thet
 cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *out, cudaStream_t st)
 {
     k_trial_logdens<<<r.S, kLikThreads, sub_smem_bytes(r.m), st>>>(r, theta, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_draw(const double *rows, int P, int C, int level0, int n_level, const int32_t *attempt,
+                             const uint8_t *done, uint64_t seed, double *theta, cudaStream_t st)
+{
+    const int64_t n = (int64_t)n_level * C * P;
+    if (n == 0) return cudaSuccess;
+    k_init_draw<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rows, P, C, level0, n_level, attempt, done, seed, theta);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,9 @@ def lib():
     L.ggdmc_logprior.argtypes = [P(abi.Prior), P(C.c_double), C.c_int32, P(C.c_double)]
     L.ggdmc_logprior_noalloc.restype = St
     L.ggdmc_logprior_noalloc.argtypes = [P(abi.Prior), P(C.c_double), C.c_int32, P(C.c_double)]
+    L.ggdmc_initialise.restype = St
+    L.ggdmc_initialise.argtypes = [C.c_void_p, P(abi.Prior), P(abi.Prior), C.c_int32, C.c_int32,
+                                   C.c_uint64, C.c_int32, P(abi.ChainState), P(abi.ChainState)]
     L.ggdmc_loghlike.restype = St
     L.ggdmc_loghlike.argtypes = [P(abi.Prior), P(C.c_double), P(C.c_double), C.c_int32,
                                  C.c_int32, P(C.c_double)]
@@ -142,6 +145,23 @@ class Handle:
                       stream: int = 0):
         check(lib().ggdmc_loglik_device(self.h, C.c_void_p(d_theta_ptr), n_theta, precision,
                                         C.c_void_p(d_out_ptr), C.c_void_p(stream)))
+
+    def initialise(self, p_table, h_table=None, nchain=3, max_attempts=200, seed=0,
+                   precision=abi.FP64):
+        """Start states drawn from the priors (initialise_theta / _phi):
+        ((theta [S][C][P], lp, ll), phi (theta [C][2P], lp, ll) or None)."""
+        m = abi.Marshal()
+        cp = m.prior(p_table)
+        ch = m.prior(h_table) if h_table is not None else None
+        S, P = self.batch.n_subject, self.model.n_par
+        st, th, lp, ll = m.states(np.zeros((S, nchain, P)), np.zeros((S, nchain)), np.zeros((S, nchain)))
+        pst = None
+        if h_table is not None:
+            pst, pth, plp, pll = m.states(np.zeros((1, nchain, 2 * P)), np.zeros((1, nchain)),
+                                          np.zeros((1, nchain)))
+        check(lib().ggdmc_initialise(self.h, C.byref(cp), C.byref(ch) if ch is not None else None,
+                                     nchain, max_attempts, C.c_uint64(seed), precision, st, pst))
+        return (th, lp, ll), ((pth[0], plp[0], pll[0]) if h_table is not None else None)
 
     def trial_logdens(self, theta, precision=abi.FP64):
         """theta [S][P] -> per-trial log densities [N]."""

@@ -264,6 +264,21 @@ ggdmc_status ggdmc_loghlike(const ggdmc_prior *p_prior, const double *phi,
                             const double *subj_theta, int32_t n_subject,
                             int32_t n, double *out);
 
+/* initialise_theta / initialise_phi (R/phi.R:141-332): start states by
+ * rejection from the priors.  Chain c of every subject takes the first of
+ * max_attempts draws from p_prior with a finite prior and likelihood; with
+ * h_prior (2 x n_par rows), each phi chain c then the first draw from h_prior
+ * with a finite prior and hyper log-likelihood against the subjects' chains
+ * c.  Draws are keyed by (seed, iteration 0, level, attempt, chain, parameter)
+ * -- R's rprior stream cannot be reproduced -- and mapped through the prior's
+ * inverse distribution function.  subj_state [n_subject] / phi_state receive
+ * theta, lp and ll; GGDMC_ERR_NUMERIC if a chain found no start. */
+ggdmc_status ggdmc_initialise(ggdmc_handle *h, const ggdmc_prior *p_prior,
+                              const ggdmc_prior *h_prior, int32_t nchain,
+                              int32_t max_attempts, uint64_t seed, int32_t precision,
+                              ggdmc_chain_state *subj_state,
+                              ggdmc_chain_state *phi_state);
+
 /* Run on a resident handle: level layout as ggdmc_run (phi_state == NULL
  * runs the subjects as independent fits, like ggdmc_run_subjects). */
 ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg,

@@ -49,6 +49,9 @@ def lib():
         L.oracle_tnorm_logpdf.argtypes = [C.c_double] * 5
         L.oracle_lba_dens.restype = C.c_double
         L.oracle_lba_dens.argtypes = [C.c_double, P(C.c_double), C.c_int, C.c_int]
+        L.oracle_initialise.restype = C.c_int
+        L.oracle_initialise.argtypes = [P(abi.Model), P(abi.Data), P(abi.Prior), P(abi.Prior), C.c_int32,
+                                        C.c_int32, C.c_uint64, P(abi.ChainState), P(abi.ChainState)]
         L.oracle_ddm_dens.restype = C.c_double
         L.oracle_ddm_dens.argtypes = [C.c_double, P(C.c_double), C.c_int]
         L.oracle_run_subject.argtypes = [P(abi.DEConfig), P(abi.Model), P(abi.Data),
@@ -80,6 +83,26 @@ def sumloglike(model, rt, cell, theta, per_trial=False):
     s = lib().oracle_sumloglike(C.byref(cm), abi.dptr(rt), abi.i32ptr(cell), len(rt),
                                 abi.dptr(th), abi.dptr(pt) if per_trial else None)
     return (s, pt[:len(rt)].copy()) if per_trial else s
+
+
+def initialise(model, batch, p_table, h_table, nchain, max_attempts, seed):
+    """Start states by rejection from the priors (initialise_theta /
+    initialise_phi): ((theta [S][C][P], lp, ll), phi (theta, lp, ll) or None)."""
+    m = abi.Marshal()
+    cm, cd, cp = m.model(model), m.data(batch), m.prior(p_table)
+    ch = m.prior(h_table) if h_table is not None else None
+    S, P = batch.n_subject, model.n_par
+    st, th, lp, ll = m.states(np.zeros((S, nchain, P)), np.zeros((S, nchain)), np.zeros((S, nchain)))
+    pst = None
+    if h_table is not None:
+        pst, pth, plp, pll = m.states(np.zeros((1, nchain, h_table.shape[0])), np.zeros((1, nchain)),
+                                      np.zeros((1, nchain)))
+    L = lib()
+    s = L.oracle_initialise(C.byref(cm), C.byref(cd), C.byref(cp), C.byref(ch) if ch is not None else None,
+                            nchain, max_attempts, C.c_uint64(seed), st, pst)
+    if s != 0:
+        raise RuntimeError(f"oracle_initialise failed with status {s}")
+    return (th, lp, ll), ((pth[0], plp[0], pll[0]) if h_table is not None else None)
 
 
 def ddm_dens(rt, cv, w):

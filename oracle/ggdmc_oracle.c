@@ -790,6 +790,95 @@ EXPORT ggdmc_status oracle_loghlike(const ggdmc_prior *p_prior, const double *ph
     return GGDMC_OK;
 }
 
+/* ------------------------------------------------------------ start states
+ * initialise_theta / initialise_phi (R/phi.R:141-332): chain c of subject s
+ * takes the first of max_attempts draws from p_prior whose prior and
+ * likelihood are both finite; then each phi chain c the first draw from
+ * h_prior whose prior and hyper log-likelihood against the subjects' chains
+ * c are finite.  R draws with rprior; here draw j of attempt a of chain c at
+ * level v (0 phi, 1 + s subject s) is the prior's inverse distribution
+ * function at the keyed uniform (iteration 0, level v, pass a, slot
+ * c * npar + j) -- iteration 0 is never used by the sampler. */
+static double Phi_inv(double p)
+{
+    /* bisection to a bracket, then Newton on Phi (erfc-based) */
+    double lo = -40.0, hi = 40.0, x = 0.0;
+    for (int it = 0; it < 60; ++it) {
+        x = 0.5 * (lo + hi);
+        if (Phi(x) < p) lo = x; else hi = x;
+    }
+    for (int it = 0; it < 3; ++it) {
+        double f = Phi(x) - p, d = exp(-0.5 * x * x) * 0.39894228040143267794;
+        if (!(d > 0.0)) break;
+        x -= f / d;
+    }
+    return x;
+}
+
+static double prior_draw(const double *row, double u)
+{
+    if ((int)row[4] == GGDMC_PRIOR_UNIF) return row[0] + u * (row[1] - row[0]);
+    double mu = row[0], sg = row[1], lo = row[2], hi = row[3];
+    double pa = isinf(lo) ? 0.0 : Phi((lo - mu) / sg), pb = isinf(hi) ? 1.0 : Phi((hi - mu) / sg);
+    double x = mu + sg * Phi_inv(pa + u * (pb - pa));
+    if (x < lo) x = lo;
+    if (x > hi) x = hi;
+    return x;
+}
+
+EXPORT ggdmc_status oracle_initialise(const ggdmc_model *m, const ggdmc_data *data,
+                                      const ggdmc_prior *p_prior, const ggdmc_prior *h_prior,
+                                      int32_t nchain, int32_t max_attempts, uint64_t seed,
+                                      ggdmc_chain_state *subj, ggdmc_chain_state *phi)
+{
+    const int P = p_prior->n_par, S = data->n_subject;
+    draw_ctx d = {NULL, seed, 1, 1, 1};
+    double *cv = malloc(sizeof(double) * m->n_cell * m->n_acc * m->n_kind);
+    double th[1024];
+    for (int s = 0; s < S; ++s) {
+        int64_t a0 = data->offsets[s], b0 = data->offsets[s + 1];
+        for (int c = 0; c < nchain; ++c) {
+            int ok = 0;
+            for (int a = 0; a < max_attempts && !ok; ++a) {
+                for (int j = 0; j < P; ++j)
+                    th[j] = prior_draw(p_prior->table + 6 * j, U(&d, 0, 1 + s, a, (int64_t)c * P + j));
+                double lp = sumlogprior(p_prior, th);
+                double ll = isfinite(lp) ? subject_sumloglike(m, data->rt + a0, data->cell + a0, b0 - a0, th, cv, NULL)
+                                         : -INFINITY;
+                if (isfinite(lp) && isfinite(ll)) {
+                    memcpy(subj[s].theta + (size_t)c * P, th, sizeof(double) * P);
+                    subj[s].lp[c] = lp;
+                    subj[s].ll[c] = ll;
+                    ok = 1;
+                }
+            }
+            if (!ok) { free(cv); return GGDMC_ERR_NUMERIC; }
+        }
+    }
+    free(cv);
+    if (!phi || !h_prior) return GGDMC_OK;
+    const int H = h_prior->n_par;
+    for (int c = 0; c < nchain; ++c) {
+        int ok = 0;
+        for (int a = 0; a < max_attempts && !ok; ++a) {
+            for (int j = 0; j < H; ++j)
+                th[j] = prior_draw(h_prior->table + 6 * j, U(&d, 0, 0, a, (int64_t)c * H + j));
+            double lp = sumlogprior(h_prior, th);
+            double ll = 0.0;
+            for (int s = 0; s < S && isfinite(lp); ++s)
+                ll += sumlogprior_phi(p_prior, th, subj[s].theta + (size_t)c * P);
+            if (isfinite(lp) && isfinite(ll)) {
+                memcpy(phi->theta + (size_t)c * H, th, sizeof(double) * H);
+                phi->lp[c] = lp;
+                phi->ll[c] = ll;
+                ok = 1;
+            }
+        }
+        if (!ok) return GGDMC_ERR_NUMERIC;
+    }
+    return GGDMC_OK;
+}
+
 EXPORT double oracle_tnorm_logpdf(double x, double mu, double sigma, double lo, double hi)
 {
     return tnorm_logpdf(x, mu, sigma, lo, hi);
