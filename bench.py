@@ -100,9 +100,31 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def make_workload():
+def single_lba(seed: int = 0, n: int = 768):
+    """One subject of the 13-parameter design, 768 trials, U(0, 10) priors,
+    39 chains: the single-subject configuration."""
+    from ggdmc_gb300.design import BV13_POP_MEAN, design_bv13, vector
+    from ggdmc_gb300.dmi import SubjectBatch
+    rng = np.random.default_rng(seed)
+    model = design_bv13()
+    th = vector(model, BV13_POP_MEAN)
+    sub = synth.simulate_subject(model, th, n, rng, "1")
+    return synth.Workload("single_lba_768", model, SubjectBatch.pack([sub]), th[None],
+                          synth.unif_prior(model.n_par), None, None, None, 3 * model.n_par, False)
+
+
+WORKLOADS = {
+    "uneven_lba_256": synth.uneven_lba_256,
+    "single_lba_768": single_lba,
+    "hier_lba_32": synth.hier_lba_32,
+    "hier_ddm_64": synth.hier_ddm_64,
+    "many_fits_1024": synth.many_fits_1024,
+}
+
+
+def make_workload(name=WORKLOAD):
     t = time.time()
-    w = synth.uneven_lba_256()
+    w = WORKLOADS[name]()
     log(f"workload {w.name}: {w.batch.n_subject} subjects, {len(w.batch.rt)} trials, "
         f"{w.nchain} chains ({time.time() - t:.1f}s to simulate)")
     return w
@@ -115,13 +137,16 @@ def start_state(w, gpu, h):
     S = w.batch.n_subject
     lp = np.stack([gpu.logprior(w.p_prior, th[s]) for s in range(S)])
     ll = h.loglik(th, abi.FP64)
+    if phi is None:
+        return None, (th, lp, ll)
     plp = gpu.logprior(w.h_prior, phi)
     pll = gpu.loghlike(w.p_prior, phi, th.transpose(0, 1, 2))
     return (phi, plp, pll), (th, lp, ll)
 
 
 def cfg_for(w, steps, precision, flags=0, seed=2025):
-    return abi.DEConfigPy(nchain=w.nchain, nparameter=2 * w.model.n_par, nmc=steps + 1, thin=1,
+    npar = 2 * w.model.n_par if w.hierarchical else w.model.n_par
+    return abi.DEConfigPy(nchain=w.nchain, nparameter=npar, nmc=steps + 1, thin=1,
                           pop_migration_prob=0.05, sub_migration_prob=0.06, precision=precision,
                           seed=seed, flags=flags)
 
@@ -183,8 +208,9 @@ def cpu_baseline(w, n_sweeps=1, threads=None):
     S = w.batch.n_subject
     lp = np.stack([ob.logprior(w.p_prior, th[s]) for s in range(S)])
     ll = ob.loglik(w.model, w.batch, th)
-    plp = ob.logprior(w.h_prior, phi)
-    pll = ob.loghlike(w.p_prior, phi, th)
+    if phi is not None:
+        plp = ob.logprior(w.h_prior, phi)
+        pll = ob.loghlike(w.p_prior, phi, th)
     cfg = cfg_for(w, n_sweeps, abi.FP64)
     threads = threads or os.cpu_count() or 1
     times = [0.0] * threads
@@ -192,7 +218,10 @@ def cpu_baseline(w, n_sweeps=1, threads=None):
     def one(k):
         c = abi.DEConfigPy(**{**cfg.__dict__, "seed": 1000 + k})
         t0 = time.perf_counter()
-        ob.run(c, w.model, w.batch, w.p_prior, w.h_prior, (phi, plp, pll), (th, lp, ll))
+        if phi is not None:
+            ob.run(c, w.model, w.batch, w.p_prior, w.h_prior, (phi, plp, pll), (th, lp, ll))
+        else:
+            ob.run_subjects(c, w.model, w.batch, w.p_prior, th, lp, ll)
         times[k] = time.perf_counter() - t0
 
     ts = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
@@ -204,7 +233,7 @@ def cpu_baseline(w, n_sweeps=1, threads=None):
     wall = time.perf_counter() - t0
     sweeps = threads * n_sweeps
     return {"value": sweeps / wall, "unit": "DE sweeps/s", "cores": threads, "kind": "port",
-            "sample": f"{threads} replicas x {n_sweeps} sweep(s) of the full {WORKLOAD} "
+            "sample": f"{threads} replicas x {n_sweeps} sweep(s) of the full {w.name} "
                       f"workload, oracle/ FP64 C restatement, one thread each",
             "wall_s": wall, "single_replica_s": float(np.median(times)),
             "trial_logl_evals_per_s": sweeps * w.nchain * len(w.batch.rt) / wall}
@@ -218,14 +247,15 @@ def run_ours(args):
         torch.distributed.init_process_group("nccl")
         torch.cuda.set_device(local)
     build.build()
-    w = make_workload()
+    w = make_workload(args.workload)
+    default = args.workload == WORKLOAD
     h = gpu.Handle(w.model, w.batch)
     phi, subj = start_state(w, gpu, h)
     peak_fp32, peak_mufu = gpu.probe_peaks()
 
     # warm-up (also compiles nothing: the library is prebuilt)
     wu = cfg_for(w, args.warmup, abi.MIXED, abi.FLAG_L2_FLUSH)
-    h.run(wu, w.p_prior, *subj, h_table=w.h_prior, phi=phi)
+    h.run(wu, w.p_prior, *subj, h_table=w.h_prior, phi=phi)   # (phi None: independent fits)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -250,12 +280,27 @@ def run_ours(args):
 
     # plain FP64 one-launch-per-subject form (the comparison the target names)
     n_plain = max(2, min(args.steps, 4))
-    pl = h.run(cfg_for(w, n_plain, abi.FP64_PLAIN, abi.FLAG_L2_FLUSH), w.p_prior, *subj,
-               h_table=w.h_prior, phi=phi)["stats"]
-    plain_sweeps_s = n_plain / (pl["sweep_ms"] / 1e3)
+    plain_sweeps_s = None
+    if default:
+        pl = h.run(cfg_for(w, n_plain, abi.FP64_PLAIN, abi.FLAG_L2_FLUSH), w.p_prior, *subj,
+                   h_table=w.h_prior, phi=phi)["stats"]
+        plain_sweeps_s = n_plain / (pl["sweep_ms"] / 1e3)
     fb = h.run(cfg_for(w, n_plain, abi.FP64, abi.FLAG_L2_FLUSH), w.p_prior, *subj,
                h_table=w.h_prior, phi=phi)["stats"]
     fp64_sweeps_s = n_plain / (fb["sweep_ms"] / 1e3)
+    if not default:
+        line = {"metric": "DE sweeps/s", "value": round(sweeps_s, 3), "unit": "DE sweeps/s",
+                "workload": w.name, "subjects": w.batch.n_subject, "trials": int(len(w.batch.rt)),
+                "chains": w.nchain, "hierarchical": w.hierarchical, "steps": args.steps,
+                "ms_per_step": round(ms / args.steps, 4),
+                "trial_logl_evals_per_s": round(evals_s, 1),
+                "fp64_batched_sweeps_per_s": round(fp64_sweeps_s, 3),
+                "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
+                "clocks": clk.summary()}
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(w, 1)
+        print(json.dumps(line), flush=True)
+        return
 
     # likelihood kernel roofline (live)
     lk_ms, lk_evals = loglik_roofline(w, h)
@@ -377,6 +422,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS),
+                    help="another configuration, reported in a reduced line (default: the "
+                         "256-subject uneven workload of the contract line)")
     ap.add_argument("--profile", action="store_true",
                     help="warm-up and timed sweeps only (for ncu launch lists and captures)")
     args = ap.parse_args()
