@@ -294,6 +294,7 @@ def run_ours(args):
                 "chains": w.nchain, "hierarchical": w.hierarchical, "steps": args.steps,
                 "ms_per_step": round(ms / args.steps, 4),
                 "trial_logl_evals_per_s": round(evals_s, 1),
+                "fp64_fallback_fraction": round(st["fallbacks"] / max(st["trial_evals"], 1), 6),
                 "fp64_batched_sweeps_per_s": round(fp64_sweeps_s, 3),
                 "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
                 "clocks": clk.summary()}
@@ -344,6 +345,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": "flushed between sweeps (256 MB memset, excluded from the timing)"},
         "trial_logl_evals_per_s": round(evals_s * world, 1),
+        "fp64_fallback_fraction": round(st["fallbacks"] / max(st["trial_evals"], 1), 6),
         "fp64_plain_sweeps_per_s": round(plain_sweeps_s, 3),
         "fp64_batched_sweeps_per_s": round(fp64_sweeps_s, 3),
         "speedup_vs_fp64_plain": round(sweeps_s / plain_sweeps_s, 2),

@@ -110,6 +110,24 @@ __device__ __forceinline__ double lba_logdens64(double t, const int *ents, int K
     return log(d);
 }
 
+// The winner's density in FP32.  When both normal arguments are >= 0 the
+// density is a sum of same-sign upper-tail terms, each relative-accurate in
+// FP32 (Mills-ratio tails), so a small density is exact enough; only one
+// within 0.1% of the reference's 1e-10 floor is re-evaluated (the floor
+// decision must agree), and one below is floored here.  Otherwise (a slow
+// response) the two terms cancel to leading order and a density below 1e-8
+// is re-evaluated in FP64.
+__device__ __forceinline__ bool winner_pdf_usable(bool fast, float &pdf)
+{
+    if (!fast) return pdf >= 1e-8f;
+    if (pdf > 1.001e-10f) return true;
+    if (pdf < 0.999e-10f) {       // also 0 and underflowed tails
+        pdf = 1e-10f;
+        return true;
+    }
+    return false;                  // near the floor, or NaN
+}
+
 // ------------------------------------------------------ FP32 LBA trial
 // e32a[u] = (beta = b/s, betam = (b-A)/s, kappa = v/s, cs = s/(A Phi(v/s)))
 // e32b[u] = (cv = v/(A Phi(v/s)), q = Phi(-v/s)/Phi(v/s))
@@ -127,14 +145,17 @@ __device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int 
     if (!(t > 1e-4f)) return false;
     const float it = __frcp_rn(t);
     float pdf;
+    bool pdf_ok;
     {
         const float4 a = e32a[ents[w]];
         const float2 b = e32b[ents[w]];
         const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
         const float pz = phi32(cz), pm = phi32(czm);
-        const float sg = (czm >= 0.f) ? -1.f : 1.f;
+        const bool fast = czm >= 0.f;
+        const float sg = fast ? -1.f : 1.f;
         const float d = sg * (ncdf32(sg * cz, pz) - ncdf32(sg * czm, pm));
         pdf = fmaf(b.x, d, a.w * (pm - pz));
+        pdf_ok = winner_pdf_usable(fast, pdf);
     }
     float surv = 1.f;
     bool bad = false;
@@ -156,7 +177,7 @@ __device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int 
         bad |= late ? !(S >= 1e-9f && S * 32.f >= b.y) : !(S >= 1e-2f);
     }
     const float d = pdf * surv;
-    if (bad || !(pdf >= 1e-8f) || !(d > 0.f) || !(d < 3.0e38f)) return false;
+    if (bad || !pdf_ok || !(d >= 1.2e-38f) || !(d < 3.0e38f)) return false;
     ld = __logf(d);
     return true;
 }
@@ -170,14 +191,17 @@ __device__ __forceinline__ bool lba_logdens32_k(float t, const int (&ent)[K], co
     if (!(t > 1e-4f)) return false;
     const float it = __frcp_rn(t);
     float pdf;
+    bool pdf_ok;
     {
         const float4 a = e32a[ent[0]];
         const float2 b = e32b[ent[0]];
         const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
         const float pz = phi32(cz), pm = phi32(czm);
-        const float sg = (czm >= 0.f) ? -1.f : 1.f;
+        const bool fast = czm >= 0.f;
+        const float sg = fast ? -1.f : 1.f;
         const float d = sg * (ncdf32(sg * cz, pz) - ncdf32(sg * czm, pm));
         pdf = fmaf(b.x, d, a.w * (pm - pz));
+        pdf_ok = winner_pdf_usable(fast, pdf);
     }
     float surv = 1.f;
     bool bad = false;
@@ -196,7 +220,7 @@ __device__ __forceinline__ bool lba_logdens32_k(float t, const int (&ent)[K], co
         bad |= late ? !(S >= 1e-9f && S * 32.f >= b.y) : !(S >= 1e-2f);
     }
     const float d = pdf * surv;
-    if (bad || !(pdf >= 1e-8f) || !(d > 0.f) || !(d < 3.0e38f)) return false;
+    if (bad || !pdf_ok || !(d >= 1.2e-38f) || !(d < 3.0e38f)) return false;
     ld = __logf(d);
     return true;
 }

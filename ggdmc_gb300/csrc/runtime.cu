@@ -851,6 +851,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         a.stats->trial_evals = (int64_t)hs[ST_TRIALS];
         a.stats->resolve_rounds = (int64_t)hs[ST_ROUNDS];
         a.stats->variants = (int64_t)hs[ST_VARIANTS];
+        a.stats->fallbacks = (int64_t)hs[ST_FALLBACKS];
         a.stats->iterations = n_iter;
         a.stats->sweep_ms = sweep_ms;
     }

@@ -24,7 +24,7 @@ enum LoopKind : int32_t {
 constexpr int kPriorRow = 6;
 
 enum StatIdx { ST_PROPOSALS = 0, ST_ACCEPTS, ST_MIGRATIONS, ST_REEVALS, ST_TRIALS, ST_ROUNDS,
-               ST_VARIANTS, ST_N };
+               ST_VARIANTS, ST_FALLBACKS, ST_N };
 
 // Migration steps evaluated ahead per in-CTA round under the assumption that
 // the steps before them accept (a migration cascade carries one value

@@ -331,11 +331,15 @@ struct SubSmem {
     int *flag;       // [kGroup] 1: FP32 form unusable for proposal g
     double *d64;     // [kGroup][n_dent][8] DDM entries (FP64)
     float *d32;      // [kGroup][n_dent][8] DDM entries (FP32; [3],[7] tshift hi, lo)
+    int *fb;         // [kFbCap] trials whose FP32 form declined: trial << 2 | proposal
+    int *fbn;        // their count
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[13])
+constexpr int kFbCap = 1024;   // FP64 re-evaluations a block lists before re-scanning its trials
+
+__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[15])
 {
     size_t o = 0;
     off[0] = o; o += sizeof(double) * kMaxTheta * kGroup;
@@ -354,18 +358,21 @@ __host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[
     o = align_up(o, 16);
     off[11] = o; o += sizeof(double) * 8 * m.n_dent * kGroup;
     off[12] = o; o += sizeof(float) * 8 * m.n_dent * kGroup;
+    o = align_up(o, 16);
+    off[13] = o; o += sizeof(int) * kFbCap;
+    off[14] = o; o += sizeof(int) * 4;
     return align_up(o, 16);
 }
 
 __host__ __device__ size_t sub_smem_bytes(const DevModel &m)
 {
-    size_t off[13];
+    size_t off[15];
     return sub_smem_layout(m, off);
 }
 
 __device__ SubSmem carve(char *base, const DevModel &m)
 {
-    size_t off[13];
+    size_t off[15];
     sub_smem_layout(m, off);
     SubSmem s;
     s.theta = (double *)(base + off[0]);
@@ -381,6 +388,8 @@ __device__ SubSmem carve(char *base, const DevModel &m)
     s.flag = (int *)(base + off[10]);
     s.d64 = (double *)(base + off[11]);
     s.d32 = (float *)(base + off[12]);
+    s.fb = (int *)(base + off[13]);
+    s.fbn = (int *)(base + off[14]);
     return s;
 }
 
@@ -568,6 +577,8 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
                 ks[g] = tt;
             } else {
                 ++nfb[g];
+                const int pos = atomicAdd(sm.fbn, 1);
+                if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
             }
         }
     }
@@ -594,6 +605,7 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
         }
         return;
     }
+    if (threadIdx.x == 0) *sm.fbn = 0;
     __syncthreads();
     bool ok[kGroup];
     float ks[kGroup], kc[kGroup];
@@ -626,6 +638,8 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
                     ks[g] = tt;
                 } else {
                     ++nfb[g];
+                    const int pos = atomicAdd(sm.fbn, 1);
+                    if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
                 }
             }
         }
@@ -639,9 +653,22 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
             continue;
         }
         build_tables64(r, sm, sm.theta + g * kMaxTheta);
+        if (r.stats) {
+            const int nf = usable ? nfb[g] : (threadIdx.x == 0 ? n : 0);
+            if (nf) atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)nf);
+        }
         __syncthreads();
         double acc = usable ? (double)ks[g] - (double)kc[g] : 0.0;
-        if (!usable || nfb[g] > 0) {
+        const int fbn = *sm.fbn;
+        if (usable && fbn <= kFbCap) {
+            // only the listed trials of proposal g
+            for (int q = threadIdx.x; q < fbn; q += blockDim.x) {
+                const int e = sm.fb[q];
+                if ((e & 3) != g) continue;
+                const int i = e >> 2;
+                acc += trial64(r, sm, base + i, r.cell[base + i], K);
+            }
+        } else if (!usable || nfb[g] > 0) {
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int c = r.cell[base + i];
                 if (usable) {

@@ -140,6 +140,7 @@ typedef struct {
     double sweep_ms;           /* device time of the sweeps (CUDA events), ms */
     int64_t resolve_rounds;    /* ordered-decision rounds over all subject passes */
     int64_t variants;          /* migration steps evaluated ahead of their decision */
+    int64_t fallbacks;         /* MIXED: trial densities re-evaluated in FP64 */
 } ggdmc_run_stats;
 
 typedef struct ggdmc_handle ggdmc_handle;
