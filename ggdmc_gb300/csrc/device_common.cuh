@@ -302,34 +302,53 @@ __device__ __forceinline__ double ddm_logdens64(double rt, const double *p)
 }
 
 // FP32 form of the same density: the series lengths from the same bounds
-// evaluated in FP32, the terms and the node sum in FP32.  Returns false
-// (re-evaluate in FP64) below 1e-8, where the 1e-10 floor is near, or when
-// a value is not finite.
-__device__ __forceinline__ float nf_density32(float tt, float w)
+// evaluated in FP32, the terms and the node sum in FP32.  The series choice,
+// its length and the large-time exponentials depend on the decision time
+// only, so they are formed once per non-decision-time node and shared by the
+// start-point nodes.  Returns false (re-evaluate in FP64) below 1e-8, where
+// the 1e-10 floor is near, or when a value is not finite.
+struct Nf32 {
+    bool small;          // small-time series
+    int K;               // its length
+    float i2t, norm;     // small time: 1 / (2 tt), (2 pi tt^3)^-1/2
+    float ek[8];         // large time: k exp(-k^2 pi^2 tt / 2), k = 1..8
+    float c;             // large time: pi^2 tt / 2 (terms past 8)
+};
+
+__device__ __forceinline__ void nf32_prepare(float tt, Nf32 &q)
 {
     const float pi = 3.14159265f;
-    float ks, kl;
     const float ek = pi * tt * 1e-10f;
-    kl = (ek < 1.f) ? fmaxf(sqrtf(-2.f * __logf(ek) / (pi * pi * tt)), 1.f / (pi * sqrtf(tt)))
-                    : 1.f / (pi * sqrtf(tt));
+    const float kl = (ek < 1.f) ? fmaxf(sqrtf(-2.f * __logf(ek) / (pi * pi * tt)), 1.f / (pi * sqrtf(tt)))
+                                : 1.f / (pi * sqrtf(tt));
     const float es = 2.f * sqrtf(2.f * pi * tt) * 1e-10f;
-    ks = (es < 1.f) ? fmaxf(2.f + sqrtf(-2.f * tt * __logf(es)), sqrtf(tt) + 1.f) : 2.f;
-    float p = 0.f;
-    if (ks < kl) {
-        const int K = (int)ceilf(ks);
-        const float i2t = 0.5f / tt;
-        for (int k = -((K - 1) / 2); k <= (K - 1) / 2; ++k) {
-            const float x = w + 2.f * k;
-            p = fmaf(x, expf(-(x * x) * i2t), p);
-        }
-        p *= rsqrtf(2.f * pi * tt * tt * tt);
-    } else {
-        const int K = (int)ceilf(kl);
-        const float c = pi * pi * tt * 0.5f;
-        for (int k = 1; k <= K; ++k) p = fmaf((float)k * expf(-(float)(k * k) * c), sinpif(k * w), p);
-        p *= pi;
+    const float ks = (es < 1.f) ? fmaxf(2.f + sqrtf(-2.f * tt * __logf(es)), sqrtf(tt) + 1.f) : 2.f;
+    q.small = ks < kl;
+    q.K = (int)ceilf(q.small ? ks : kl);
+    q.i2t = 0.5f / tt;
+    q.norm = rsqrtf(2.f * pi * tt * tt * tt);
+    q.c = pi * pi * tt * 0.5f;
+    if (!q.small) {
+#pragma unroll
+        for (int k = 1; k <= 8; ++k) q.ek[k - 1] = (float)k * expf(-(float)(k * k) * q.c);
     }
-    return p;
+}
+
+__device__ __forceinline__ float nf32_eval(const Nf32 &q, float w)
+{
+    float p = 0.f;
+    if (q.small) {
+        for (int k = -((q.K - 1) / 2); k <= (q.K - 1) / 2; ++k) {
+            const float x = w + 2.f * k;
+            p = fmaf(x, expf(-(x * x) * q.i2t), p);
+        }
+        return p * q.norm;
+    }
+#pragma unroll
+    for (int k = 1; k <= 8; ++k)
+        if (k <= q.K) p = fmaf(q.ek[k - 1], sinpif(k * w), p);
+    for (int k = 9; k <= q.K; ++k) p = fmaf((float)k * expf(-(float)(k * k) * q.c), sinpif(k * w), p);
+    return p * 3.14159265f;
 }
 
 __device__ __forceinline__ bool ddm_logdens32(float rt_hi, float rt_lo, const float *p, float &ld)
@@ -346,10 +365,12 @@ __device__ __forceinline__ bool ddm_logdens32(float rt_hi, float rt_lo, const fl
         if (!(tt > 0.f)) continue;
         const float den = fmaf(sv2, tt, 1.f);
         const float rden = rsqrtf(den), hden = 0.5f / den;
+        Nf32 q;
+        nf32_prepare(tt * ia2, q);
         float part = 0.f;
         for (int iz = 0; iz < nz; ++iz) {
             const float zz = (nz > 1) ? fmaf(sz, (iz + 0.5f) / nz - 0.5f, zr) : zr;
-            const float g = nf_density32(tt * ia2, zz) * ia2;
+            const float g = nf32_eval(q, zz) * ia2;
             const float aw = a * zz;
             const float e = (fmaf(sv2 * aw, aw, -2.f * v * aw) - v * v * tt) * hden;
             part = fmaf(g, expf(e), part);
