@@ -215,6 +215,31 @@ def test_edge_empty_subject_and_floor(oracle):
     assert np.allclose(got, want, rtol=1e-12)
 
 
+def test_mixed_many_fallbacks_in_one_block(oracle):
+    # one subject of 3000 trials with t0 above a large share of its RTs: most
+    # trials leave the FP32 form (t < 1e-4), more than a block lists, so the
+    # block re-scans its trials; sums still match the FP64 oracle
+    from ggdmc_gb300.design import T0_17_P, design_t0_17, vector
+    rng = np.random.default_rng(21)
+    model = design_t0_17()
+    th = vector(model, T0_17_P)
+    sub = synth.simulate_subject(model, th, 3000, rng, "1")
+    batch = SubjectBatch.pack([sub])
+    bad = th.copy()
+    for j, nm in enumerate(model.pnames):
+        if nm.startswith("t0"):
+            bad[j] = np.quantile(sub.rt, 0.6)
+    theta = np.stack([th, bad])[None]                  # [1][2][P]
+    h = gpu.Handle(model, batch)
+    want = oracle.loglik(model, batch, theta)
+    mixed = h.loglik(theta, abi.MIXED)
+    assert np.all(rel(mixed, want) <= 1e-6), rel(mixed, want)
+    run = h.run(abi.DEConfigPy(nchain=3, nparameter=model.n_par, nmc=2, thin=1, seed=1,
+                               precision=abi.MIXED), synth.unif_prior(model.n_par),
+                np.stack([bad] * 3)[None], np.zeros((1, 3)), h.loglik(np.stack([bad] * 3)[None], abi.MIXED))
+    assert run["stats"]["fallbacks"] > 1024
+
+
 def test_invalid_inputs_are_errors():
     z, model, sub, _ = load_fixture(6)
     bad = SubjectBatch(sub.rt[:5], np.full(5, model.n_cell + 3, np.int32), np.array([0, 5]))
