@@ -154,38 +154,8 @@ __device__ __forceinline__ double tnorm_const_p(const RunDev &r, double mu, doub
     return (r.prec == PREC_MIXED) ? tnorm_const_mixed(mu, sigma, lo, hi) : tnorm_const(mu, sigma, lo, hi);
 }
 
-// Subject-level prior: fixed table, or the truncated normal of phi chain
-// `phi_chain` (src/de.cpp:599-603, 646-652).
-__device__ double sub_prior(const RunDev &r, const double *th, int phi_chain)
-{
-    double s = 0.0;
-    if (r.prior) {
-        for (int j = 0; j < r.P; ++j) s += prior_term(r.prior + kPriorRow * j, th[j]);
-    } else {
-        const double *pt = r.phi_tab + (size_t)phi_chain * r.P * 3;   // (mu, 1/sigma, c)
-        for (int j = 0; j < r.P; ++j) {
-            const double x = th[j];
-            double term;
-            if (x < r.pp_bounds[2 * j] || x > r.pp_bounds[2 * j + 1] || !(pt[3 * j + 1] > 0.0)) {
-                term = -INFINITY;
-            } else {
-                const double z = (x - pt[3 * j]) * pt[3 * j + 1];
-                term = -0.5 * z * z + pt[3 * j + 2];
-            }
-            s += term;
-        }
-    }
-    return s;
-}
-
-__device__ __forceinline__ double phi_prior(const RunDev &r, const double *th)
-{
-    double s = 0.0;
-    for (int j = 0; j < r.Pphi; ++j) s += prior_term(r.hprior + kPriorRow * j, th[j]);
-    return s;
-}
-
-// phi_prior with the warp's lanes over the parameters; every lane gets the sum.
+// The phi level's prior (h_prior), the warp's lanes over the parameters;
+// every lane gets the sum.
 __device__ __forceinline__ double warp_phi_prior(const RunDev &r, const double *th)
 {
     double s = 0.0;
@@ -297,21 +267,6 @@ __device__ __forceinline__ double cross_comp(double gamma, double ti, double ta,
 __device__ __forceinline__ bool updated(int j, int para, int nloop)
 {
     return (para >= 0) ? (j == para) : (j < nloop);
-}
-
-// Re-proposals from the current state with the pass's stored jitter.
-__device__ __forceinline__ void cross_prop_j(double gamma, int para, int nloop, int P,
-                                             const double *ti, const double *ta, const double *tb,
-                                             const double *jit, double *out)
-{
-    for (int j = 0; j < P; ++j)
-        out[j] = updated(j, para, nloop) ? cross_comp(gamma, ti[j], ta[j], tb[j], jit[j]) : ti[j];
-}
-
-__device__ __forceinline__ void mig_prop_j(int para, int nloop, int P, const double *ts,
-                                           const double *jit, double *out)
-{
-    for (int j = 0; j < P; ++j) out[j] = updated(j, para, nloop) ? __dadd_rn(ts[j], jit[j]) : ts[j];
 }
 
 // --------------------------------------------------- subject likelihood
@@ -1085,7 +1040,6 @@ __host__ __device__ inline size_t jit_stage_bytes(int C, int P)
     return b <= kJitStage ? b : 0;
 }
 
-
 // Copy the rows of the steps accepted by the last scan into the state.
 __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na, bool lead)
 {
@@ -1439,7 +1393,6 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
         atomicAdd(&r.stats[ST_ROUNDS], (unsigned long long)rounds);
     }
 }
-
 
 // k_sub_resolve: one CTA per level of [level_begin, level_begin + n_level),
 // block q taking level order[q] (largest first; nullptr: index order), so
