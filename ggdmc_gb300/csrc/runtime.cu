@@ -155,6 +155,7 @@ struct ggdmc_handle {
     DevBuf<double> consts;
     // trials
     int S = 0;
+    int last_nmc = 0, last_C = 0, last_P = 0, last_Pphi = 0, last_S = 0;   // samples left by the last run
     std::vector<int64_t> h_offs;
     DevBuf<int64_t> offs;
     DevBuf<double> rt64;
@@ -842,6 +843,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     if ((s = wait_stream(st))) return s;
     if (dev_status)
         return fail(GGDMC_ERR_TIMEOUT, "a device-side wait gave up (code " + std::to_string(dev_status) + ")");
+    h->last_nmc = nmc; h->last_C = C; h->last_P = P; h->last_Pphi = Pphi; h->last_S = S;
     if (a.stats) {
         a.stats->proposals = (int64_t)hs[ST_PROPOSALS];
         a.stats->accepts = (int64_t)hs[ST_ACCEPTS];
@@ -1153,6 +1155,36 @@ ggdmc_status ggdmc_initialise(ggdmc_handle *h, const ggdmc_prior *p_prior, const
     std::memcpy(phi_state->lp, plp.data(), sizeof(double) * C);
     std::memcpy(phi_state->ll, pll.data(), sizeof(double) * C);
     return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_handle_summary(ggdmc_handle *h, int32_t start, double *mean, double *sd, double *psrf,
+                                  double *phi_mean, double *phi_sd, double *phi_psrf)
+{
+    if (!h) return fail(GGDMC_ERR_ARG, "handle is NULL");
+    if (h->last_nmc < 1) return fail(GGDMC_ERR_ARG, "no run has stored samples on this handle");
+    const int nmc = h->last_nmc, C = h->last_C;
+    if (start < 0 || nmc - start < 2 || C < 2)
+        return fail(GGDMC_ERR_ARG, "summary needs two or more iterations after start and two or more chains");
+    cudaStream_t st = h->stream;
+    auto level = [&](const double *smp, int L, int P, double *m, double *s, double *r) -> ggdmc_status {
+        if (L < 1 || P < 1) return GGDMC_OK;
+        if (!m || !s || !r) return fail(GGDMC_ERR_ARG, "summary output is NULL");
+        DevBuf<double> cs, dm, dsd, dr;
+        CU(cs.alloc((size_t)L * C * P * 2));
+        CU(dm.alloc((size_t)L * P));
+        CU(dsd.alloc((size_t)L * P));
+        CU(dr.alloc((size_t)L * P));
+        CU(launch_summary(smp, L, nmc, C, P, start, cs.p, dm.p, dsd.p, dr.p, st));
+        CU(cudaMemcpyAsync(m, dm.p, sizeof(double) * L * P, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(s, dsd.p, sizeof(double) * L * P, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(r, dr.p, sizeof(double) * L * P, cudaMemcpyDeviceToHost, st));
+        return wait_stream(st);
+    };
+    ggdmc_status s = level(h->smp_th.p, h->last_S, h->last_P, mean, sd, psrf);
+    if (s) return s;
+    if (h->last_Pphi > 0 && phi_mean)
+        s = level(h->psmp_th.p, 1, h->last_Pphi, phi_mean, phi_sd, phi_psrf);
+    return s;
 }
 
 ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta, int32_t precision, double *out)

@@ -121,6 +121,8 @@ cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *o
                                  cudaStream_t st);
 cudaError_t launch_init_draw(const double *rows, int P, int C, int level0, int n_level, const int32_t *attempt,
                              const uint8_t *done, uint64_t seed, double *theta, cudaStream_t st);
+cudaError_t launch_summary(const double *smp, int L, int nmc, int C, int P, int start, double *cs,
+                           double *mean, double *sd, double *psrf, cudaStream_t st);
 cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
                             cudaStream_t st);
 cudaError_t launch_loghlike(const RunDev &r, const double *phi, double *out, cudaStream_t st);

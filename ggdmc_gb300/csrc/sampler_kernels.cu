@@ -2134,6 +2134,82 @@ cudaError_t launch_init_draw(const double *rows, int P, int C, int level0, int n
     return cudaGetLastError();
 }
 
+// Posterior summaries of stored samples (summary / gelman, R/model-class.R:
+// 370-424, 1559-1690): level l's samples smp [l][nmc][C][P], iterations
+// [start, nmc).  Phase 1: per (chain, parameter) the mean and variance
+// (Welford, coalesced over the (chain, parameter) pairs of an iteration)
+// into cs [l][C][P][2]; phase 2: per parameter the pooled mean and sd and
+// the potential scale reduction factor's point estimate in Brooks & Gelman's
+// form as coda computes it (chains as the replicates; needs C >= 2).
+__global__ void k_summary(const double *smp, int nmc, int C, int P, int start, double *cs,
+                          double *mean, double *sd, double *psrf)
+{
+    const int l = blockIdx.x;
+    const int n = nmc - start;
+    const double *x = smp + (size_t)l * nmc * C * P;
+    double *stat = cs + (size_t)l * C * P * 2;
+    for (int q = threadIdx.x; q < C * P; q += blockDim.x) {
+        double m = 0.0, m2 = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double v = x[(size_t)(start + i) * C * P + q];
+            const double dl = v - m;
+            m += dl / (i + 1);
+            m2 += dl * (v - m);
+        }
+        stat[2 * q] = m;
+        stat[2 * q + 1] = (n > 1) ? m2 / (n - 1) : 0.0;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        double mu = 0.0, w = 0.0;
+        for (int c = 0; c < C; ++c) {
+            mu += stat[2 * (c * P + p)];
+            w += stat[2 * (c * P + p) + 1];
+        }
+        mu /= C;
+        w /= C;
+        double b = 0.0, vw = 0.0, m2bar = 0.0;
+        for (int c = 0; c < C; ++c) {
+            const double mc = stat[2 * (c * P + p)], sc = stat[2 * (c * P + p) + 1];
+            b += (mc - mu) * (mc - mu);
+            vw += (sc - w) * (sc - w);
+            m2bar += mc * mc;
+        }
+        m2bar /= C;
+        double cov_s_m = 0.0, cov_s_m2 = 0.0;
+        for (int c = 0; c < C; ++c) {
+            const double mc = stat[2 * (c * P + p)], sc = stat[2 * (c * P + p) + 1];
+            cov_s_m += (sc - w) * (mc - mu);
+            cov_s_m2 += (sc - w) * (mc * mc - m2bar);
+        }
+        const double varm = b / (C - 1);                  // var of the chain means
+        b = n * varm;
+        const double var_w = vw / (C - 1) / C;
+        const double var_b = 2.0 * b * b / (C - 1);
+        const double cov_wb = ((double)n / C) * (cov_s_m2 / (C - 1) - 2.0 * mu * cov_s_m / (C - 1));
+        const double V = (n - 1.0) / n * w + (1.0 + 1.0 / C) / n * b;
+        const double var_V = ((n - 1.0) * (n - 1.0) * var_w + (1.0 + 1.0 / C) * (1.0 + 1.0 / C) * var_b +
+                              2.0 * (n - 1.0) * (1.0 + 1.0 / C) * cov_wb) / ((double)n * n);
+        const double df_V = 2.0 * V * V / var_V;
+        const double df_adj = (df_V + 3.0) / (df_V + 1.0);
+        const double r2 = (n - 1.0) / n + (1.0 + 1.0 / C) / n * (b / w);
+        // pooled over chains and iterations
+        const double tot = (double)n * C;
+        const double ss = (n - 1.0) * w * C + n * varm * (C - 1);
+        mean[(size_t)l * P + p] = mu;
+        sd[(size_t)l * P + p] = sqrt(ss / (tot - 1.0));
+        psrf[(size_t)l * P + p] = sqrt(df_adj * r2);
+    }
+}
+
+cudaError_t launch_summary(const double *smp, int L, int nmc, int C, int P, int start, double *cs,
+                           double *mean, double *sd, double *psrf, cudaStream_t st)
+{
+    if (L < 1) return cudaSuccess;
+    k_summary<<<L, 256, 0, st>>>(smp, nmc, C, P, start, cs, mean, sd, psrf);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
                             cudaStream_t st)
 {

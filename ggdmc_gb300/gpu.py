@@ -56,6 +56,8 @@ def lib():
     L.ggdmc_initialise.restype = St
     L.ggdmc_initialise.argtypes = [C.c_void_p, P(abi.Prior), P(abi.Prior), C.c_int32, C.c_int32,
                                    C.c_uint64, C.c_int32, P(abi.ChainState), P(abi.ChainState)]
+    L.ggdmc_handle_summary.restype = St
+    L.ggdmc_handle_summary.argtypes = [C.c_void_p, C.c_int32] + [P(C.c_double)] * 6
     L.ggdmc_loghlike.restype = St
     L.ggdmc_loghlike.argtypes = [P(abi.Prior), P(C.c_double), P(C.c_double), C.c_int32,
                                  C.c_int32, P(C.c_double)]
@@ -162,6 +164,20 @@ class Handle:
         check(lib().ggdmc_initialise(self.h, C.byref(cp), C.byref(ch) if ch is not None else None,
                                      nchain, max_attempts, C.c_uint64(seed), precision, st, pst))
         return (th, lp, ll), ((pth[0], plp[0], pll[0]) if h_table is not None else None)
+
+    def summary(self, start=0, phi=False):
+        """Posterior mean, sd and PSRF (coda's form) of the last run's samples,
+        computed on the device: {"subj": (mean, sd, psrf) [S][P], "phi": ... [2P]}."""
+        S, P = self.batch.n_subject, self.model.n_par
+        m, s, r = (np.zeros((S, P)) for _ in range(3))
+        pm, ps, pr = (np.zeros(2 * P) for _ in range(3))
+        ptr = lambda a: abi.dptr(a) if phi else None
+        check(lib().ggdmc_handle_summary(self.h, start, abi.dptr(m), abi.dptr(s), abi.dptr(r),
+                                         ptr(pm), ptr(ps), ptr(pr)))
+        out = {"subj": (m, s, r)}
+        if phi:
+            out["phi"] = (pm, ps, pr)
+        return out
 
     def trial_logdens(self, theta, precision=abi.FP64):
         """theta [S][P] -> per-trial log densities [N]."""

@@ -280,6 +280,16 @@ ggdmc_status ggdmc_initialise(ggdmc_handle *h, const ggdmc_prior *p_prior,
                               ggdmc_chain_state *subj_state,
                               ggdmc_chain_state *phi_state);
 
+/* summary / gelman (R/model-class.R:370-424, 1559-1690) of the samples the
+ * last ggdmc_handle_run left on the device, without copying them: for
+ * iterations [start, nmc), per subject and parameter the posterior mean, sd
+ * and the potential scale reduction factor's point estimate (Brooks &
+ * Gelman's form as coda's gelman.diag computes it).  mean, sd, psrf:
+ * [n_subject][n_par]; phi_*: [2 n_par] of the phi level, or NULL. */
+ggdmc_status ggdmc_handle_summary(ggdmc_handle *h, int32_t start, double *mean,
+                                  double *sd, double *psrf, double *phi_mean,
+                                  double *phi_sd, double *phi_psrf);
+
 /* Run on a resident handle: level layout as ggdmc_run (phi_state == NULL
  * runs the subjects as independent fits, like ggdmc_run_subjects). */
 ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg,
