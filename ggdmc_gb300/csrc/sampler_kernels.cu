@@ -108,6 +108,43 @@ __device__ __forceinline__ double block_sum_ff(float h, float l, double *red)
     return out;
 }
 
+// block_sum_ff of the group's ng (h, l) pairs at once: one exchange through
+// shared memory, warp g reducing pair g.  Every thread gets out[0..ng).
+template <int G>
+__device__ __forceinline__ void block_sum_ff_group(const float (&h)[G], const float (&l)[G], int ng,
+                                                   double *red, double *out)
+{
+    float *rf = (float *)red;                     // [G][32] (h, l) pairs
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        if (g >= ng) break;
+        float hh = h[g], ll = l[g];
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
+            ff_add(hh, ll, h2, l2);
+        }
+        if (lane == 0) { rf[2 * (g * 32 + wid)] = hh; rf[2 * (g * 32 + wid) + 1] = ll; }
+    }
+    __syncthreads();
+    double *res = red + G * 32;
+    for (int g = wid; g < ng; g += nw) {
+        float hh = (lane < nw) ? rf[2 * (g * 32 + lane)] : 0.f;
+        float ll = (lane < nw) ? rf[2 * (g * 32 + lane) + 1] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
+            ff_add(hh, ll, h2, l2);
+        }
+        if (lane == 0) res[g] = (double)hh + (double)ll;
+    }
+    __syncthreads();
+    for (int g = 0; g < ng; ++g) out[g] = res[g];
+    __syncthreads();
+}
+
 __device__ __forceinline__ double prior_term(const double *row, double x)
 {
     const int id = (int)row[0];
@@ -276,7 +313,7 @@ struct SubSmem {
     double *theta;   // [kGroup][kMaxTheta]
     double *e64;     // n_ent * 5
     double *t064;    // n_t0
-    double *red;     // 33
+    double *red;     // 165: block reductions
     float4 *e32a;    // [kGroup][n_ent]
     float2 *e32b;    // [kGroup][n_ent]
     float2 *t032;    // [kGroup][n_t0]
@@ -300,7 +337,7 @@ __host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[
     off[0] = o; o += sizeof(double) * kMaxTheta * kGroup;
     off[1] = o; o += sizeof(double) * 5 * m.n_ent;
     off[2] = o; o += sizeof(double) * m.n_t0;
-    off[3] = o; o += sizeof(double) * 33;
+    off[3] = o; o += sizeof(double) * (33 + 4 * 32 + 4);   // block_sum / block_sum_ff_group
     o = align_up(o, 16);
     off[4] = o; o += sizeof(float4) * m.n_ent * kGroup;
     off[5] = o; o += sizeof(float2) * m.n_ent * kGroup;
@@ -598,6 +635,18 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
                 }
             }
         }
+    }
+    // no FP64 work anywhere in the group: one fused reduction
+    bool anyfb = false;
+#pragma unroll
+    for (int g = 0; g < kGroup; ++g)
+        if (g < ng) anyfb |= nfb[g] > 0 || sm.flag[g] != 0;
+    if (!__syncthreads_or(anyfb)) {
+        float nkc[kGroup];
+#pragma unroll
+        for (int g = 0; g < kGroup; ++g) nkc[g] = -kc[g];
+        block_sum_ff_group(ks, nkc, ng, sm.red, out);
+        return;
     }
 #pragma unroll
     for (int g = 0; g < kGroup; ++g) {
