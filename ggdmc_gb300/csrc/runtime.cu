@@ -165,7 +165,7 @@ struct ggdmc_handle {
     DevBuf<double> th, lp, ll, th_s, lp_s, ll_s, phi_tab, pp_bounds, prior, hprior, hrows;
     DevBuf<double> pth, plp, pll, pth_s, plp_s, pll_s, pref_src, pref_next;
     DevBuf<int32_t> partner, ptype, nstep, sub, migrated, ppartner, pptype, pnstep, psub,
-        pmigrated, iter, status, items, items_plain, rs_para, sub_order;
+        pmigrated, iter, status, items, items_plain, rs_para, sub_order, ready, spec_cnt, ctl;
     DevBuf<int8_t> need, pneed;
     DevBuf<float4> tab_a;
     DevBuf<float2> tab_b, tab_t;
@@ -589,6 +589,27 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     CU(cudaMemsetAsync(h->stats.p, 0, sizeof(unsigned long long) * ST_N, st));
     CU(cudaMemsetAsync(h->iter.p, 0, sizeof(int32_t), st));
     CU(cudaMemsetAsync(h->status.p, 0, sizeof(int32_t), st));
+    // The subject pass fused with the next iteration's proposals
+    // (k_sub_step) needs one subject pass per iteration and not the plain
+    // form.  It pays where the levels come in several waves per SM and no
+    // phi level waits for the pass: the next iteration's evaluations then
+    // fill the SMs the ordered decisions leave idle.  With a phi level the
+    // phi update of t + 1 can only start after the whole pass, and the
+    // speculative evaluations already run beside it.  GGDMC_FUSED=0/1
+    // overrides the choice.
+    const int sub_npass = hier ? (c.is_pblocked ? c.nparameter / 2 : 1) : (c.is_pblocked ? c.nparameter : 1);
+    const bool fusable = S > 0 && !plain && sub_npass == 1;
+    bool fused = fusable && !hier && Pphi == 0 && S >= 2 * h->n_sm;
+    if (const char *fs = std::getenv("GGDMC_FUSED")) fused = fusable && std::atoi(fs) != 0;
+    if (fused) {
+        CU(h->ready.alloc(S));
+        CU(h->spec_cnt.alloc(S));
+        CU(h->ctl.alloc(3));
+        CU(cudaMemsetAsync(h->ready.p, 0xff, sizeof(int32_t) * S, st));   // -1: no iteration
+
+        CU(cudaMemsetAsync(h->spec_cnt.p, 0, sizeof(int32_t) * S, st));
+        CU(cudaMemsetAsync(h->ctl.p, 0, sizeof(int32_t) * 3, st));
+    }
 
     // ---- run description
     RunDev r{};
@@ -633,6 +654,10 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.psmp_th = h->psmp_th.p; r.psmp_lp = h->psmp_lp.p; r.psmp_ll = h->psmp_ll.p;
     r.stats = h->stats.p;
     r.status = h->status.p;
+    r.ready = fused ? h->ready.p : nullptr;
+    r.spec_cnt = fused ? h->spec_cnt.p : nullptr;
+    r.ctl = fused ? h->ctl.p : nullptr;
+    r.iter_end = (int32_t)n_iter;
 
     int64_t launches_per_iter = 0;
     // One DE iteration (src/de.cpp:201-242 / 272-383) as a launch sequence.
@@ -643,12 +668,17 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         // (only their priors do), so they run on a second stream beside it,
         // at low priority so the phi level's small kernels get SMs first;
         // k_sub_resolve scores the priors after the join.
+        // Fused: k_sub_step of the previous iteration has already built
+        // this iteration's proposals and evaluated part of them; the propose
+        // kernel skips those levels and k_sub_spec_rest takes the items left.
         const bool fork = hier && S > 0 && Pphi > 0 && !plain;
         if (fork) {
             if ((e = cudaEventRecord(h->ev_fork, st))) return e;
             if ((e = cudaStreamWaitEvent(h->stream2, h->ev_fork, 0))) return e;
-            if ((e = launch_sub_propose(r, 0, true, h->stream2))) return e;
-            if ((e = launch_sub_loglik(r, h->items.p, n_spec_items, spec_group, h->stream2))) return e;
+            if ((e = launch_sub_propose(r, 0, true, fused, h->stream2))) return e;
+            if (fused) e = launch_sub_spec_rest(r, spec_group, h->stream2);
+            else e = launch_sub_loglik(r, h->items.p, n_spec_items, spec_group, h->stream2);
+            if (e) return e;
             if ((e = cudaEventRecord(h->ev_join, h->stream2))) return e;
             launches_per_iter += 2;
         }
@@ -672,11 +702,20 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             for (int p = 0; p < npass; ++p) {
                 if (fork && p == 0) {
                     if ((e = cudaStreamWaitEvent(st, h->ev_join, 0))) return e;
-                    if ((e = launch_sub_resolve(r, 0, 0, S, true, st))) return e;
+                    if (fused) e = launch_sub_step(r, true, true, spec_group, st);
+                    else e = launch_sub_resolve(r, 0, 0, S, true, st);
+                    if (e) return e;
                     ++launches_per_iter;
                     continue;
                 }
-                if ((e = launch_sub_propose(r, p, false, st))) return e;
+                if (fused) {
+                    if ((e = launch_sub_propose(r, p, false, true, st))) return e;
+                    if ((e = launch_sub_spec_rest(r, spec_group, st))) return e;
+                    if ((e = launch_sub_step(r, false, false, spec_group, st))) return e;
+                    launches_per_iter += 3;
+                    continue;
+                }
+                if ((e = launch_sub_propose(r, p, false, false, st))) return e;
                 ++launches_per_iter;
                 if (plain) {
                     for (int l = 0; l < S; ++l) {

@@ -98,13 +98,22 @@ struct RunDev {
     double *smp_th, *smp_lp, *smp_ll;     // [S][nmc][C][P], [S][nmc][C]
     double *psmp_th, *psmp_lp, *psmp_ll;  // [nmc][C][Pphi], [nmc][C]
 
+    // k_sub_step / k_sub_spec_rest (subject pass fused with the next
+    // iteration's proposals)
+    int32_t *ready;                // [S] iteration whose proposals level l holds
+    int32_t *spec_cnt;             // [S] spec items of the level claimed so far
+    int32_t *ctl;                  // [3] levels claimed / resolved this pass, events
+    int32_t iter_end;              // last iteration of the run
+
     unsigned long long *stats;     // [ST_N]
     int32_t *status;
 };
 
 // --------------------------------------------------------------- launchers
 // (defined in sampler_kernels.cu)
-cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, cudaStream_t st);
+cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, bool fused, cudaStream_t st);
+cudaError_t launch_sub_spec_rest(const RunDev &r, int group, cudaStream_t st);
+cudaError_t launch_sub_step(const RunDev &r, bool score_priors, bool defer_next, int group, cudaStream_t st);
 cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items, int group,
                               cudaStream_t st);
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,

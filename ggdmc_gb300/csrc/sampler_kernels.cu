@@ -20,6 +20,7 @@
 // states equal the sequential sampler's.
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cstdio>
 #include <cstdint>
 
@@ -46,6 +47,8 @@ constexpr int kResolveThreads = GGDMC_RESOLVE_THREADS;
 constexpr int kMigRound = 8;              // migration variants evaluated per resolve round
 constexpr int kPhiThreads = 256;
 constexpr int kProposeThreads = 512;
+// k_sub_step's claim counters (RunDev::ctl)
+constexpr int kCtlResNext = 0, kCtlResDone = 1, kCtlEvents = 2, kCtlN = 3;
 constexpr int kPhiProposeThreads = 1024;   // one CTA: a warp per phi chain's prior
 
 // ------------------------------------------------------------- helpers
@@ -456,17 +459,27 @@ __device__ void build_tables32(const RunDev &r, SubSmem &sm, int g)
 
 // Load proposal slot `slot` (theta and, in MIXED, its stored FP32 tables)
 // as group member g.
+// Global load; CO: through L2 only, for data another CTA of the running
+// kernel wrote (published by a release/acquire pair on a flag).
+template <bool CO, class T>
+__device__ __forceinline__ T ldx(const T *p)
+{
+    if constexpr (CO) return __ldcg(p);
+    else return *p;
+}
+
+template <bool CO = false>
 __device__ void load_slot(const RunDev &r, size_t slot, SubSmem &sm, int g, bool mixed)
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0;
-    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[g * kMaxTheta + j] = r.th_s[slot * r.P + j];
+    for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[g * kMaxTheta + j] = ldx<CO>(r.th_s + slot * r.P + j);
     if (!mixed) return;
     for (int u = threadIdx.x; u < NE; u += blockDim.x) {
-        sm.e32a[g * NE + u] = r.tab_a[slot * NE + u];
-        sm.e32b[g * NE + u] = r.tab_b[slot * NE + u];
+        sm.e32a[g * NE + u] = ldx<CO>(r.tab_a + slot * NE + u);
+        sm.e32b[g * NE + u] = ldx<CO>(r.tab_b + slot * NE + u);
     }
-    for (int q = threadIdx.x; q < NT; q += blockDim.x) sm.t032[g * NT + q] = r.tab_t[slot * NT + q];
-    if (threadIdx.x == 0) sm.flag[g] = r.tab_bad[slot];
+    for (int q = threadIdx.x; q < NT; q += blockDim.x) sm.t032[g * NT + q] = ldx<CO>(r.tab_t + slot * NT + q);
+    if (threadIdx.x == 0) sm.flag[g] = ldx<CO>(r.tab_bad + slot);
 }
 
 // Trial log density of proposal g in FP64 (the reference form).
@@ -692,13 +705,14 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
 
 // Evaluate the log-likelihoods of proposal slots `slots[0..m)` of level l on
 // the whole CTA, kGroup at a time; results to ll_s (and to lls[k] when given).
+template <bool CO = false>
 __device__ void eval_slots(const RunDev &r, int l, const int *slots, int m, SubSmem &sm, bool mixed,
                            double *lls_sm)
 {
     const int N = (int)(r.offs[l + 1] - r.offs[l]);
     for (int g0 = 0; g0 < m; g0 += kGroup) {
         const int ng = min(kGroup, m - g0);
-        for (int g = 0; g < ng; ++g) load_slot(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
+        for (int g = 0; g < ng; ++g) load_slot<CO>(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
         __syncthreads();
         double out[kGroup];
         group_loglik(r, l, 0, N, sm, ng, mixed, out);
@@ -765,17 +779,27 @@ __device__ __forceinline__ bool in_support(const RunDev &r, const double *th)
     return true;
 }
 
-__global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int pass, int defer_prior)
+// Shared scratch of propose_level: (C + 2) uniforms (reused for the
+// migration cascade, hence at least P), then four int arrays of C.
+__host__ __device__ inline int prop_cap(int C, int P) { return (C + 2 > P) ? C + 2 : P; }
+__host__ __device__ inline size_t prop_scratch_bytes(int C, int P)
 {
-    __shared__ double s_u[kMaxChain + 2];
-    __shared__ int s_sub[kMaxChain];
-    __shared__ int s_perm[kMaxChain];
-    __shared__ int s_pa[kMaxChain], s_pb[kMaxChain];
+    return sizeof(double) * (size_t)prop_cap(C, P) + sizeof(int) * 4 * (size_t)C;
+}
+
+// Pass type, partners, stored draws and proposals of subject level l for
+// iteration `it` (the body of k_sub_propose; all threads of the CTA).
+template <bool CO = false>
+__device__ void propose_level(const RunDev &r, int l, int64_t it, int pass, bool defer_prior, char *scratch)
+{
     __shared__ int s_type, s_n, s_para;
-    const int l = blockIdx.x;
     const int lev = r.level0 + l;
-    const int64_t it = *r.iter;
     const int C = r.C, P = r.P, CS = r.CS;
+    double *s_u = (double *)scratch;
+    int *s_sub = (int *)(s_u + prop_cap(C, P));
+    int *s_perm = s_sub + C;
+    int *s_pa = s_perm + C;
+    int *s_pb = s_pa + C;
     if (threadIdx.x == 0) {
         int type = PASS_CROSS, para = -1;
         if (r.loop == LOOP_HCHAINS) {
@@ -839,13 +863,14 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
     for (int q = threadIdx.x; q < n * P; q += blockDim.x) {
         const int k = q / P, j = q % P;
         const int src = (type == PASS_CROSS) ? k : s_sub[k];
-        const double ts = th[(size_t)src * P + j];
+        const double ts = ldx<CO>(th + (size_t)src * P + j);
         double out = ts;
         if (updated(j, para, nloop)) {
             const double jv = jitter_draw(r, it, lev, pass, k, j);
             jit[(size_t)k * P + j] = jv;
             out = (type == PASS_CROSS)
-                      ? cross_comp(r.gamma, ts, th[(size_t)s_pa[k] * P + j], th[(size_t)s_pb[k] * P + j], jv)
+                      ? cross_comp(r.gamma, ts, ldx<CO>(th + (size_t)s_pa[k] * P + j),
+                                   ldx<CO>(th + (size_t)s_pb[k] * P + j), jv)
                       : __dadd_rn(ts, jv);
         }
         ths[(size_t)k * P + j] = out;
@@ -876,14 +901,14 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
         // the running sums in shared memory (s_u, whose draws are consumed),
         // then one parallel store; jit was written above by this block
         double *s_v = s_u;
-        constexpr int kCap = kMaxChain + 2;
+        const int kCap = prop_cap(C, P);
         for (int w0 = 0; w0 < nv; w0 += kCap / P) {
             const int wn = min(nv - w0, kCap / P);
             __syncthreads();
             for (int q = threadIdx.x; q < wn * P; q += blockDim.x) s_v[q] = jit[(size_t)(w0 + q / P) * P + q % P];
             __syncthreads();
             for (int j = threadIdx.x; j < P; j += blockDim.x) {
-                double v = (w0 == 0) ? th[(size_t)s_sub[0] * P + j] : ths[(size_t)(C + w0 - 1) * P + j];
+                double v = (w0 == 0) ? ldx<CO>(th + (size_t)s_sub[0] * P + j) : ths[(size_t)(C + w0 - 1) * P + j];
                 const bool up = updated(j, para, nloop);
                 for (int w = 0; w < wn; ++w) {
                     if (up) v = __dadd_rn(v, s_v[w * P + j]);
@@ -925,6 +950,26 @@ __global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int p
     }
 }
 
+// grid = S.  fused: a level k_sub_step already proposed for this iteration
+// (ready[l] == iteration) is skipped, and a level proposed here gets its
+// spec-item counter cleared and its ready stamp; block 0 also clears
+// k_sub_step's claim counters.
+__global__ void __launch_bounds__(kProposeThreads) k_sub_propose(RunDev r, int pass, int defer_prior, int fused)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const int l = blockIdx.x;
+    const int it = *r.iter;
+    if (fused) {
+        if (l == 0 && threadIdx.x < kCtlN) r.ctl[threadIdx.x] = 0;
+        if (r.ready[l] == it) return;
+    }
+    propose_level(r, l, it, pass, defer_prior != 0, smem_raw);
+    if (fused && threadIdx.x == 0) {
+        r.spec_cnt[l] = 0;
+        r.ready[l] = it;
+    }
+}
+
 // k_sub_loglik: the hot kernel.  One CTA per work item = up to kGroup
 // proposals of one subject, items in descending trial-count order (longest
 // first keeps the tail short).  item = level * CS + first slot.
@@ -948,6 +993,62 @@ __global__ void __launch_bounds__(kLikThreads, GGDMC_LIK_MINB) k_sub_loglik(RunD
     SubSmem sm = carve(smem_raw, r.m);
     load_design(r, sm);
     eval_slots(r, l, s_slots, s_m, sm, r.prec == PREC_MIXED, nullptr);
+}
+
+// Spec item k of level l: the crossover steps [k g, k g + g) for k < ceil(C / g),
+// then the migration cascade slots C + [..).  Writes the slots that need an
+// evaluation to slots[] and returns their count (one thread).
+template <bool CO>
+__device__ int spec_item_slots(const RunDev &r, int l, int k, int group, int *slots)
+{
+    const int nic = (r.C + group - 1) / group;
+    const int n = ldx<CO>(r.nstep + l);
+    int k0, kend;
+    if (k < nic) {
+        k0 = k * group;
+        kend = min(n, k0 + group);
+    } else {
+        k0 = r.C + (k - nic) * group;
+        kend = min(r.C + n, k0 + group);
+    }
+    int m = 0;
+    for (int q = k0; q < kend; ++q)
+        if (ldx<CO>(r.need + (size_t)l * r.CS + q)) slots[m++] = q;
+    return m;
+}
+
+// k_sub_spec_rest: the spec items k_sub_step left unclaimed.  blocks_per_level
+// CTAs per level (levels largest first), each claiming items from the level's
+// counter until none is left.
+__global__ void __launch_bounds__(kLikThreads, GGDMC_LIK_MINB)
+k_sub_spec_rest(RunDev r, int group, int blocks_per_level)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    __shared__ int s_slots[kGroup];
+    __shared__ int s_m, s_k;
+    const int l = r.sub_order[blockIdx.x / blocks_per_level];
+    const int n_item = 2 * ((r.C + group - 1) / group);
+    SubSmem sm = carve(smem_raw, r.m);
+    bool loaded = false;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int k, m = 0;
+            do {
+                k = atomicAdd(r.spec_cnt + l, 1);
+                if (k < n_item) m = spec_item_slots<false>(r, l, k, group, s_slots);
+            } while (k < n_item && m == 0);
+            s_k = k;
+            s_m = m;
+        }
+        __syncthreads();
+        if (s_k >= n_item) return;
+        if (!loaded) {
+            load_design(r, sm);
+            loaded = true;
+        }
+        eval_slots(r, l, s_slots, s_m, sm, r.prec == PREC_MIXED, nullptr);
+        __syncthreads();
+    }
 }
 
 // Evaluate slots[0..m) of subject l over all its trials, kGroup at a time;
@@ -1456,6 +1557,106 @@ k_sub_resolve(RunDev r, int level_begin, int n_level, const int32_t *order, int 
     load_design(r, sm);
     __syncthreads();
     resolve_level(r, level_begin + (order ? order[q] : q), sm, smem_raw, score_priors != 0);
+}
+
+// k_sub_step: the subject pass of iteration t (= *iter) and the start of
+// iteration t + 1's, on a persistent grid.  CTAs claim levels largest first
+// and resolve them; the CTA that resolved level l then builds l's proposals
+// for t + 1 (they read only l's state) and publishes them (ready[l] = t + 1).
+// Once every level is claimed, CTAs evaluate spec items of published levels
+// while any level is still being resolved, and leave the rest to
+// k_sub_spec_rest, which runs beside the phi level of t + 1.  An idle CTA
+// polls one event counter (bumped by every publication and every resolved
+// level); its waits are only for levels a running CTA holds, and bounded.
+constexpr int kSpecIdleLimit = 1 << 21;     // idle polls (~1 us each)
+constexpr int kStatusSpecWait = 3;
+
+__device__ __forceinline__ int vload(const int32_t *p) { return *(const volatile int32_t *)p; }
+
+__global__ void __launch_bounds__(kResolveThreads, GGDMC_RESOLVE_MINB)
+k_sub_step(RunDev r, int score_priors, int defer_next, int group)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    __shared__ int s_q, s_m, s_state;
+    __shared__ int s_slots[kGroup];
+    SubSmem sm = carve(smem_raw, r.m);
+    load_design(r, sm);
+    __syncthreads();
+    const int it = *r.iter;
+    const bool next = it < r.iter_end;
+    // propose_level's scratch: the resolve's region, free once a level is decided
+    char *scratch = smem_raw + sub_smem_bytes(r.m);
+    for (;;) {
+        if (threadIdx.x == 0) s_q = atomicAdd(r.ctl + kCtlResNext, 1);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();
+        if (q >= r.S) break;
+        const int l = r.sub_order[q];
+        resolve_level(r, l, sm, smem_raw, score_priors != 0);
+        __syncthreads();
+        if (next) {
+            propose_level(r, l, it + 1, 0, defer_next != 0, scratch);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                r.spec_cnt[l] = 0;
+                __threadfence();
+                atomicExch(r.ready + l, it + 1);
+            }
+        }
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(r.ctl + kCtlResDone, 1);
+            atomicAdd(r.ctl + kCtlEvents, 1);
+        }
+    }
+    if (!next) return;
+    const bool mixed = r.prec == PREC_MIXED;
+    const int n_item = 2 * ((r.C + group - 1) / group);
+    int seen = -1;                 // event count of the last fruitless scan
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // 0: every level resolved, 1: scan, 2: gave up waiting
+            int st = 1;
+            for (int idle = 0;; ++idle) {
+                if (vload(r.ctl + kCtlResDone) >= r.S) { st = 0; break; }
+                if (vload(r.ctl + kCtlEvents) != seen) break;
+                if (idle > kSpecIdleLimit) {
+                    atomicExch(r.status, kStatusSpecWait);
+                    st = 2;
+                    break;
+                }
+                __nanosleep(1000);
+            }
+            s_state = st;
+            s_q = INT_MAX;
+            s_m = 0;
+        }
+        __syncthreads();
+        if (s_state != 1) break;
+        const int ev = vload(r.ctl + kCtlEvents);        // before the scan
+        // the first published level (largest first) with an unclaimed item
+        for (int q = threadIdx.x; q < r.S; q += blockDim.x) {
+            const int l = r.sub_order[q];
+            if (vload(r.ready + l) == it + 1 && vload(r.spec_cnt + l) < n_item) atomicMin(&s_q, q);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && s_q != INT_MAX) {
+            const int l = r.sub_order[s_q];
+            if (vload(r.ready + l) == it + 1) {
+                __threadfence();                      // acquire l's proposals
+                const int k = atomicAdd(r.spec_cnt + l, 1);
+                if (k < n_item) s_m = spec_item_slots<true>(r, l, k, group, s_slots);
+            }
+        }
+        __syncthreads();
+        if (s_q == INT_MAX) {
+            seen = ev;             // nothing to take: wait for the next event
+            continue;
+        }
+        if (s_m > 0) eval_slots<true>(r, r.sub_order[s_q], s_slots, s_m, sm, mixed, nullptr);
+    }
 }
 
 // ------------------------------------------------------------ phi level
@@ -2094,14 +2295,49 @@ cudaError_t configure_kernels(const DevModel &m)
     if ((e = cudaFuncSetAttribute(k_sub_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   bytes + (int)res_smem_bytes(kMaxChain) + (int)kJitStage)))
         return e;
+    if ((e = cudaFuncSetAttribute(k_sub_spec_rest, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    const size_t step_extra = std::max(res_smem_bytes(kMaxChain) + kJitStage, prop_scratch_bytes(kMaxChain, kMaxTheta));
+    if ((e = cudaFuncSetAttribute(k_sub_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  bytes + (int)step_extra)))
+        return e;
     if ((e = cudaFuncSetAttribute(k_loglik_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
     return cudaFuncSetAttribute(k_trial_logdens, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, cudaStream_t st)
+cudaError_t launch_sub_propose(const RunDev &r, int pass, bool defer_prior, bool fused, cudaStream_t st)
 {
-    k_sub_propose<<<r.S, kProposeThreads, 0, st>>>(r, pass, defer_prior ? 1 : 0);
+    k_sub_propose<<<r.S, kProposeThreads, prop_scratch_bytes(r.C, r.P), st>>>(r, pass, defer_prior ? 1 : 0,
+                                                                            fused ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_spec_rest(const RunDev &r, int group, cudaStream_t st)
+{
+    const int bpl = (r.C + group - 1) / group;
+    k_sub_spec_rest<<<r.S * bpl, kLikThreads, sub_smem_bytes(r.m), st>>>(r, group, bpl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sub_step(const RunDev &r, bool score_priors, bool defer_next, int group, cudaStream_t st)
+{
+    const size_t smem = sub_smem_bytes(r.m) + std::max(res_smem_bytes(r.C) + jit_stage_bytes(r.C, r.P),
+                                                       prop_scratch_bytes(r.C, r.P));
+    // persistent: at most the CTAs that fit on the device at once
+    thread_local size_t cached_smem = 0;
+    thread_local int cached_grid = 0;
+    if (cached_smem != smem) {
+        int dev = 0, n_sm = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (!e) e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sub_step, kResolveThreads, smem);
+        if (e) return e;
+        cached_grid = std::max(1, n_sm * std::max(1, per_sm));
+        cached_smem = smem;
+    }
+    const int grid = std::min(r.S, cached_grid);
+    k_sub_step<<<grid, kResolveThreads, smem, st>>>(r, score_priors ? 1 : 0, defer_next ? 1 : 0, group);
     return cudaGetLastError();
 }
 
