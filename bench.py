@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 from ggdmc_gb300 import abi, synth  # noqa: E402
 
 WORKLOAD = "uneven_lba_256"
-E2E_MAX_STEPS = 50                       # samples of every chain come back: 2.1 MB per sweep
+E2E_MAX_STEPS = 500                      # samples of every chain come back: 2.1 MB per sweep
 PROFILE = os.path.join(ROOT, "profiles", "k_loglik_batch_uneven_lba_256.md")
 K_ACC = 4
 FLOPS_PER_EVAL = 17 * K_ACC + 2          # algorithmic flops of one LBA trial density

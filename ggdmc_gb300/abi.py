@@ -124,9 +124,11 @@ class Marshal:
         return arr, theta, lp, ll
 
     def samples(self, n_level, nmc, nchain, npar):
-        theta = self.keep(np.full((n_level, nmc, nchain, npar), np.nan))
-        lp = self.keep(np.full((n_level, nmc, nchain), -np.inf))
-        ll = self.keep(np.full((n_level, nmc, nchain), -np.inf))
+        # not pre-filled: a run that returns OK writes every slot (slot 0 is the
+        # start state), and a failed run raises before they are read
+        theta = self.keep(np.empty((n_level, nmc, nchain, npar)))
+        lp = self.keep(np.empty((n_level, nmc, nchain)))
+        ll = self.keep(np.empty((n_level, nmc, nchain)))
         arr = (Samples * n_level)()
         for i in range(n_level):
             arr[i] = Samples(dptr(theta[i]), dptr(lp[i]), dptr(ll[i]))
