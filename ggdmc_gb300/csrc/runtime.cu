@@ -102,6 +102,29 @@ struct DevBuf {
     }
 };
 
+// Page-locked host buffer (grows, kept by the handle across runs).
+struct PinnedBuf {
+    char *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t bytes)
+    {
+        if (bytes <= n && p) return cudaSuccess;
+        release();
+        n = bytes;
+        return cudaHostAlloc((void **)&p, std::max<size_t>(bytes, 1), cudaHostAllocDefault);
+    }
+};
+
 double host_Phi(double z) { return 0.5 * std::erfc(-z * 0.70710678118654752440); }
 
 // Prior row (dist_id, p0, p1, lower, upper, c); see sampler.cuh.
@@ -175,6 +198,7 @@ struct ggdmc_handle {
     DevBuf<unsigned long long> stats;
     DevBuf<double> io_a, io_b;
     DevBuf<uint8_t> flushbuf;
+    PinnedBuf stage[2];                   // sample chunks on their way to the caller's buffers
 
     DevModel dev_model() const
     {
@@ -208,6 +232,24 @@ double timeout_seconds()
 }
 
 // Wait for all work on the stream with a deadline; never blocks forever.
+// Wait for an event with the GGDMC_TIMEOUT_S deadline (the host stops
+// waiting; device work already queued still runs to its end).
+ggdmc_status wait_event(cudaEvent_t ev)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const double lim = timeout_seconds();
+    int spins = 0;
+    for (;;) {
+        const cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess) return GGDMC_OK;
+        if (e != cudaErrorNotReady)
+            return fail(GGDMC_ERR_CUDA, std::string("device work failed: ") + cudaGetErrorString(e));
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > lim) return fail(GGDMC_ERR_TIMEOUT, "device work exceeded GGDMC_TIMEOUT_S");
+        if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
 ggdmc_status wait_stream(cudaStream_t st)
 {
     cudaEvent_t ev;
@@ -217,25 +259,9 @@ ggdmc_status wait_stream(cudaStream_t st)
         cudaEventDestroy(ev);
         return fail(GGDMC_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
     }
-    const auto t0 = std::chrono::steady_clock::now();
-    const double lim = timeout_seconds();
-    int spins = 0;
-    for (;;) {
-        e = cudaEventQuery(ev);
-        if (e == cudaSuccess) break;
-        if (e != cudaErrorNotReady) {
-            cudaEventDestroy(ev);
-            return fail(GGDMC_ERR_CUDA, std::string("device work failed: ") + cudaGetErrorString(e));
-        }
-        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (el > lim) {
-            cudaEventDestroy(ev);
-            return fail(GGDMC_ERR_TIMEOUT, "device work exceeded GGDMC_TIMEOUT_S");
-        }
-        if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
-    }
+    const ggdmc_status s = wait_event(ev);
     cudaEventDestroy(ev);
-    return GGDMC_OK;
+    return s;
 }
 
 // Diffusion model: two boundaries; the density of a cell depends only on the
@@ -741,6 +767,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     CU(launch_next_iter(r, st));
     int64_t launches = 2;
     double sweep_ms = 0.0;
+    int64_t copied = 0;   // sample slots already in the caller's buffers
     // cfg->flags bit 0: flush L2 (a memset larger than L2) between
     // iterations and time only the iterations' kernels, by event nodes.
     const bool flush = (c.flags & GGDMC_FLAG_L2_FLUSH) != 0;
@@ -784,6 +811,97 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         const int64_t per_iter = launches_per_iter / per_graph;
         int64_t done = 0;
         ggdmc_status ws = GGDMC_OK;
+
+        // Samples go to the caller while later sweeps run: after replay j,
+        // one strided copy per array takes the slots it stored, for every
+        // level, into page-locked stage j % 2 (second stream), and the host
+        // moves chunk j - 1 into the caller's buffers while replay j runs.
+        // Not with the L2-flush timing, which waits on every replay anyway.
+        const bool want_subj = S > 0 && a.subj_out, want_phi = Pphi > 0 && a.phi_out;
+        const bool pipe = !flush && (want_subj || want_phi);
+        const size_t rth = (size_t)C * P, rph = (size_t)C * Pphi;   // doubles per slot
+        auto slots_after = [&](int64_t iters) { return std::min<int64_t>(nmc, iters / c.thin + 1); };
+        int64_t chunk_lo[2] = {0, 0}, chunk_hi[2] = {0, 0}, enq_hi = 0, rep = 0;
+        cudaEvent_t ev_rep[2] = {}, ev_cp[2] = {};
+        auto destroy_pipe = [&]() {
+            for (int b = 0; b < 2; ++b) {
+                if (ev_rep[b]) cudaEventDestroy(ev_rep[b]);
+                if (ev_cp[b]) cudaEventDestroy(ev_cp[b]);
+            }
+        };
+        if (pipe) {
+            const int64_t ns_max = std::min<int64_t>(nmc, per_graph / c.thin + 2);
+            size_t bytes = 0;
+            if (want_subj) bytes += sizeof(double) * (size_t)S * ns_max * C * (P + 2);
+            if (want_phi) bytes += sizeof(double) * (size_t)ns_max * C * (Pphi + 2);
+            cudaError_t pe = cudaSuccess;
+            for (int b = 0; b < 2 && !pe; ++b) {
+                pe = h->stage[b].alloc(bytes);
+                if (!pe) pe = cudaEventCreateWithFlags(&ev_rep[b], cudaEventDisableTiming);
+                if (!pe) pe = cudaEventCreateWithFlags(&ev_cp[b], cudaEventDisableTiming);
+            }
+            if (pe) {
+                destroy_pipe();
+                cleanup_events();
+                cudaGraphExecDestroy(exec);
+                cudaGraphDestroy(graph);
+                return fail(GGDMC_ERR_CUDA, std::string("sample staging: ") + cudaGetErrorString(pe));
+            }
+        }
+        auto enqueue = [&](int b, int64_t lo, int64_t hi) -> cudaError_t {
+            chunk_lo[b] = lo;
+            chunk_hi[b] = hi;
+            if (hi <= lo) return cudaSuccess;
+            const size_t ns = (size_t)(hi - lo);
+            cudaStream_t s2 = h->stream2;
+            cudaError_t e = cudaStreamWaitEvent(s2, ev_rep[b], 0);
+            char *dst = h->stage[b].p;
+            const auto rows = [&](const double *src, size_t row, size_t n_row) -> cudaError_t {
+                // n_row levels of ns slots each, source pitch nmc slots
+                const size_t w = sizeof(double) * ns * row;
+                cudaError_t ce = cudaMemcpy2DAsync(dst, w, src + (size_t)lo * row, sizeof(double) * nmc * row, w,
+                                                   n_row, cudaMemcpyDeviceToHost, s2);
+                dst += w * n_row;
+                return ce;
+            };
+            if (want_subj) {
+                if (!e) e = rows(h->smp_th.p, rth, S);
+                if (!e) e = rows(h->smp_lp.p, C, S);
+                if (!e) e = rows(h->smp_ll.p, C, S);
+            }
+            if (want_phi) {
+                if (!e) e = rows(h->psmp_th.p, rph, 1);
+                if (!e) e = rows(h->psmp_lp.p, C, 1);
+                if (!e) e = rows(h->psmp_ll.p, C, 1);
+            }
+            if (!e) e = cudaEventRecord(ev_cp[b], s2);
+            return e;
+        };
+        auto drain = [&](int b) -> ggdmc_status {
+            const int64_t lo = chunk_lo[b], hi = chunk_hi[b];
+            if (hi <= lo) return GGDMC_OK;
+            ggdmc_status w = wait_event(ev_cp[b]);
+            if (w) return w;
+            const size_t ns = (size_t)(hi - lo);
+            const char *src = h->stage[b].p;
+            const auto put = [&](double *to, size_t row) {
+                if (to) std::memcpy(to + (size_t)lo * row, src, sizeof(double) * ns * row);
+                src += sizeof(double) * ns * row;
+            };
+            if (want_subj) {
+                for (int l = 0; l < S; ++l) put(a.subj_out[l].theta, rth);
+                for (int l = 0; l < S; ++l) put(a.subj_out[l].lp, C);
+                for (int l = 0; l < S; ++l) put(a.subj_out[l].ll, C);
+            }
+            if (want_phi) {
+                put(a.phi_out->theta, rph);
+                put(a.phi_out->lp, C);
+                put(a.phi_out->ll, C);
+            }
+            copied = hi;
+            return GGDMC_OK;
+        };
+
         if (!flush) CU(cudaEventRecord(ev_a[per_graph], st));
         while (done + per_graph <= n_iter && !ws) {
             cudaError_t e = cudaGraphLaunch(exec, st);
@@ -792,6 +910,20 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
                 break;
             }
             done += per_graph;
+            if (pipe) {
+                const int b = (int)(rep & 1);
+                e = cudaEventRecord(ev_rep[b], st);
+                const int64_t hi = slots_after(done);
+                if (!e) e = enqueue(b, enq_hi, hi);
+                if (e) {
+                    ws = fail(GGDMC_ERR_CUDA, std::string("sample copy: ") + cudaGetErrorString(e));
+                    break;
+                }
+                enq_hi = std::max(enq_hi, hi);
+                if (rep >= 1) ws = drain(b ^ 1);
+                ++rep;
+                continue;
+            }
             if (!flush) continue;
             // read this replay's event nodes before the next replay reuses them
             ws = wait_stream(st);
@@ -811,6 +943,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             if (!ws) cudaEventElapsedTime(&ms, ev_a[per_graph], ev_b[per_graph]);
             sweep_ms += ms;
         }
+        if (pipe && rep >= 1 && !ws) ws = drain((int)((rep - 1) & 1));
         for (; done < n_iter && !ws; ++done) {
             launches_per_iter = 0;
             cudaError_t e = cudaEventRecord(ev_a[per_graph], st);
@@ -830,6 +963,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         cudaGraphExecDestroy(exec);
         cudaGraphDestroy(graph);
         cleanup_events();
+        destroy_pipe();
         if (ws) return ws;
     }
 
@@ -845,17 +979,19 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             std::memcpy(cs.theta, buf.data() + (size_t)l * C * P, sizeof(double) * C * P);
             std::memcpy(cs.lp, b1.data() + (size_t)l * C, sizeof(double) * C);
             std::memcpy(cs.ll, b2.data() + (size_t)l * C, sizeof(double) * C);
-            if (a.subj_out) {
+            if (a.subj_out && copied < nmc) {
+                // the slots the pipelined copies have not delivered
                 const ggdmc_samples &o = a.subj_out[l];
+                const size_t k0 = (size_t)copied, nk = (size_t)(nmc - copied);
                 if (o.theta)
-                    CU(cudaMemcpyAsync(o.theta, h->smp_th.p + (size_t)l * nmc * C * P,
-                                       sizeof(double) * nmc * C * P, cudaMemcpyDeviceToHost, st));
+                    CU(cudaMemcpyAsync(o.theta + k0 * C * P, h->smp_th.p + ((size_t)l * nmc + k0) * C * P,
+                                       sizeof(double) * nk * C * P, cudaMemcpyDeviceToHost, st));
                 if (o.lp)
-                    CU(cudaMemcpyAsync(o.lp, h->smp_lp.p + (size_t)l * nmc * C,
-                                       sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+                    CU(cudaMemcpyAsync(o.lp + k0 * C, h->smp_lp.p + ((size_t)l * nmc + k0) * C,
+                                       sizeof(double) * nk * C, cudaMemcpyDeviceToHost, st));
                 if (o.ll)
-                    CU(cudaMemcpyAsync(o.ll, h->smp_ll.p + (size_t)l * nmc * C,
-                                       sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+                    CU(cudaMemcpyAsync(o.ll + k0 * C, h->smp_ll.p + ((size_t)l * nmc + k0) * C,
+                                       sizeof(double) * nk * C, cudaMemcpyDeviceToHost, st));
             }
         }
     }
@@ -864,15 +1000,18 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         CU(cudaMemcpyAsync(ps.theta, h->pth.p, sizeof(double) * C * Pphi, cudaMemcpyDeviceToHost, st));
         CU(cudaMemcpyAsync(ps.lp, h->plp.p, sizeof(double) * C, cudaMemcpyDeviceToHost, st));
         CU(cudaMemcpyAsync(ps.ll, h->pll.p, sizeof(double) * C, cudaMemcpyDeviceToHost, st));
-        if (a.phi_out) {
+        if (a.phi_out && copied < nmc) {
             const ggdmc_samples &o = *a.phi_out;
+            const size_t k0 = (size_t)copied, nk = (size_t)(nmc - copied);
             if (o.theta)
-                CU(cudaMemcpyAsync(o.theta, h->psmp_th.p, sizeof(double) * nmc * C * Pphi,
-                                   cudaMemcpyDeviceToHost, st));
+                CU(cudaMemcpyAsync(o.theta + k0 * C * Pphi, h->psmp_th.p + k0 * C * Pphi,
+                                   sizeof(double) * nk * C * Pphi, cudaMemcpyDeviceToHost, st));
             if (o.lp)
-                CU(cudaMemcpyAsync(o.lp, h->psmp_lp.p, sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+                CU(cudaMemcpyAsync(o.lp + k0 * C, h->psmp_lp.p + k0 * C, sizeof(double) * nk * C,
+                                   cudaMemcpyDeviceToHost, st));
             if (o.ll)
-                CU(cudaMemcpyAsync(o.ll, h->psmp_ll.p, sizeof(double) * nmc * C, cudaMemcpyDeviceToHost, st));
+                CU(cudaMemcpyAsync(o.ll + k0 * C, h->psmp_ll.p + k0 * C, sizeof(double) * nk * C,
+                                   cudaMemcpyDeviceToHost, st));
         }
     }
     unsigned long long hs[ST_N];
