@@ -1369,8 +1369,14 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             // evaluate the re-proposed chains whose prior is finite
             const int e = block_compact(0, m, [&](int q) { return rs.lps[rs.list[q]] > -INFINITY; },
                                         rs.acc, rs.warp);
-            for (int q = threadIdx.x; q < e; q += blockDim.x) rs.list[q] = rs.list[rs.acc[q]];
-            __syncthreads();
+            if (e < m) {
+                // through accslot (free until the next round's decisions): an
+                // in-place gather could read an entry another warp has moved
+                for (int q = threadIdx.x; q < e; q += blockDim.x) rs.accslot[q] = rs.list[rs.acc[q]];
+                __syncthreads();
+                for (int q = threadIdx.x; q < e; q += blockDim.x) rs.list[q] = rs.accslot[q];
+                __syncthreads();
+            }
             PH_ADD(c_rep);
             PH_T0();
             eval_direct(r, l, rs.list, e, sm, mixed, rs.lls, 0);
