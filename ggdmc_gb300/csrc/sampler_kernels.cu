@@ -1221,11 +1221,11 @@ __host__ __device__ inline size_t jit_stage_bytes(int C, int P)
 }
 
 // Copy the rows of the steps accepted by the last scan into the state.
-__device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na, bool lead)
+__device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &rs, int na)
 {
     const int C = r.C, P = r.P;
     const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
-    for (int q = threadIdx.x; lead && q < na * P; q += blockDim.x) {
+    for (int q = threadIdx.x; q < na * P; q += blockDim.x) {
         const int a = q / P, j = q % P;
         const int i = rs.acc[a];
         const int dst = (type == PASS_CROSS) ? i : ((i + 1 == n) ? rs.pa[0] : rs.pa[i + 1]);
@@ -1237,14 +1237,12 @@ __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &
         const int sl = rs.accslot[a];
         const double lpv = (sl < C) ? rs.lps[sl] : rs.vlp[sl - C];
         const double llv = (sl < C) ? rs.lls[sl] : rs.vll[sl - C];
-        if (lead) {
-            r.lp[lc + dst] = lpv;
-            r.ll[lc + dst] = llv;
-        }
+        r.lp[lc + dst] = lpv;
+        r.ll[lc + dst] = llv;
         rs.lp[dst] = lpv;
         rs.ll[dst] = llv;
     }
-    if (lead && threadIdx.x == 0 && na) atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)na);
+    if (threadIdx.x == 0 && na) atomicAdd(&r.stats[ST_ACCEPTS], (unsigned long long)na);
     __syncthreads();
 }
 
@@ -1259,7 +1257,6 @@ __device__ void write_accepts(const RunDev &r, int l, int type, int n, ResSmem &
 // can need.
 __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_raw, bool score_priors)
 {
-    const bool lead = true;
     const int type = r.ptype[l];
     if (type == PASS_SKIP) return;
     const int n = r.nstep[l];
@@ -1342,7 +1339,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             const int na = block_compact(dc, d, [&](int i) { return rs.dec[i] != 0; }, rs.acc, rs.warp);
             for (int q = threadIdx.x; q < na; q += blockDim.x) rs.accslot[q] = rs.acc[q];
             __syncthreads();
-            write_accepts(r, l, type, n, rs, na, lead);
+            write_accepts(r, l, type, n, rs, na);
             decided = d;
             PH_ADD(c_dec);
             if (decided >= n) break;
@@ -1373,10 +1370,8 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                 if ((threadIdx.x & 31) == 0) {
                     rs.lps[k] = lp;
                     rs.lls[k] = 0.0;
-                    if (lead) {
-                        r.lp_s[ls + k] = lp;
-                        r.ll_s[ls + k] = 0.0;
-                    }
+                    r.lp_s[ls + k] = lp;
+                    r.ll_s[ls + k] = 0.0;
                 }
             }
             if (mixed) {
@@ -1561,18 +1556,18 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             }
             __syncthreads();
             decided = rs.misc[0];
-            write_accepts(r, l, type, n, rs, rs.misc[1], lead);
+            write_accepts(r, l, type, n, rs, rs.misc[1]);
             __syncthreads();
             PH_ADD(c_dec);
         }
     }
 #ifdef GGDMC_PHASE_PROFILE
-    if (lead && threadIdx.x == 0 && *r.iter == 3)
+    if (threadIdx.x == 0 && *r.iter == 3)
         printf("PHASE l=%d type=%d N=%d n=%d reevals=%d variants=%d rounds=%d dec=%lld rep=%lld ev=%lld tot=%lld\n",
                l, type, (int)(r.offs[l + 1] - r.offs[l]), n, reevals, variants, rounds, c_dec, c_rep, c_ev,
                clock64() - t_start);
 #endif
-    if (lead && threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
         atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
         atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
         atomicAdd(&r.stats[ST_VARIANTS], (unsigned long long)variants);
