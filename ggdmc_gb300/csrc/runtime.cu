@@ -517,7 +517,12 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
 
     // ---- device buffers
     const int CS = 2 * C;   // speculative proposals, then migration variants
-    int spec_group = 4;
+    // Proposals per speculative work item (one pass over the subject's
+    // trials).  Smaller items balance the launch better.  The 4-accumulator
+    // LBA measured fastest at 2 (0.584 ms per sweep against 0.604 at 1 and
+    // 0.595 at 4), the diffusion model and the 2-accumulator fits at 1
+    // (hier_ddm_64 2.34 / 2.43 / 3.10 ms, many_fits_1024 3.44 / 3.75 / 4.56 ms).
+    int spec_group = (h->model_type == GGDMC_MODEL_DDM || h->n_acc < 4) ? 1 : 2;
     if (const char *gs = std::getenv("GGDMC_SPEC_GROUP")) spec_group = std::min(4, std::max(1, std::atoi(gs)));
     int n_spec_items = 0;
     if (S > 0) {
