@@ -121,7 +121,9 @@ typedef struct {
 } ggdmc_chain_state;
 
 /* Thinned samples of one level: posterior@theta, @summed_log_prior,
- * @log_likelihoods (R/phi.R:77-87). */
+ * @log_likelihoods (R/phi.R:77-87).  The buffers fill while the run goes
+ * on (a CUDA-graph replay's slots while the next replay runs); every slot is
+ * written when the call returns GGDMC_OK.  Any pointer may be NULL. */
 typedef struct {
     double *theta;             /* [nmc][nchain][npar] == R [npar, nchain, nmc] */
     double *lp;                /* [nmc][nchain]       == R [nchain, nmc]       */
