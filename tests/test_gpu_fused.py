@@ -82,3 +82,23 @@ def test_fused_and_unfused_agree_mixed(oracle, monkeypatch):
     assert np.allclose(a["ll"], b["ll"], rtol=0, atol=1e-4)
     for k in ("accepts", "trial_evals", "migrations", "proposals"):
         assert a["stats"][k] == b["stats"][k]
+
+
+@pytest.mark.parametrize("group", ["1", "2", "4"])
+def test_spec_group_sizes_bit_exact(oracle, monkeypatch, group):
+    # the number of proposals per speculative work item only regroups the
+    # work: each proposal's trials are summed over the same thread partition
+    monkeypatch.setenv("GGDMC_SPEC_GROUP", group)
+    z, model, _, pop = load_fixture(6)
+    S, C = 8, 26
+    batch = SubjectBatch(pop.rt[: pop.offsets[S]], pop.cell[: pop.offsets[S]],
+                         pop.offsets[: S + 1])
+    phi = (z["phi_theta"][:C], z["phi_lp"][:C], z["phi_ll"][:C])
+    subj = (z["subj_theta"][:S, :C], z["subj_lp"][:S, :C], z["subj_ll"][:S, :C])
+    cfg = abi.DEConfigPy(nchain=C, nparameter=2 * model.n_par, nmc=4, thin=1,
+                         pop_migration_prob=0.3, sub_migration_prob=0.3, seed=31)
+    g = gpu.run(cfg, model, batch, z["pop_p_prior"], z["pop_h_prior"], phi, subj)
+    o = oracle.run(cfg, model, batch, z["pop_p_prior"], z["pop_h_prior"], phi, subj)
+    assert np.array_equal(g["subj"][0], o["subj"][0])
+    assert np.array_equal(g["phi"][0], o["phi"][0])
+    assert np.allclose(g["subj"][2], o["subj"][2], rtol=1e-12)
