@@ -18,6 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libggdmc_gpu.so")
 SOURCES = ["sampler_kernels.cu", "runtime.cu", "peak.cu"]
+C_SOURCES = ["dmi_convert.c"]            # host-only C, compiled by gcc
 HEADERS = ["device_common.cuh", "model_tables.h", "sampler.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -35,7 +36,9 @@ def _stale() -> bool:
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
+    deps += [os.path.join(CSRC, f) for f in C_SOURCES]
     deps.append(os.path.join(ROOT, "include", "ggdmc_gpu.h"))
+    deps.append(os.path.join(ROOT, "include", "ggdmc_dmi.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
@@ -52,6 +55,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+        objs.append(obj)
+    for src in C_SOURCES:
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".c.o")
+        cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
         objs.append(obj)
     errors = []

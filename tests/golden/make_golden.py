@@ -11,7 +11,8 @@ when the fixture generators (``tests/testthat/Group1/data/*_lba_*.r``) ran, so
 they are known answers for the per-subject LBA log-likelihood sum, the
 truncated-normal / uniform log priors and the hyper log-likelihood.
 
-Usage (needs the reference checkout; the GPU machine does not):
+Usage (needs the reference checkout, given as an argument or by the
+GGDMC_REFERENCE environment variable; the GPU machine does not):
     python tests/golden/make_golden.py [REFERENCE_ROOT]
 """
 
@@ -78,12 +79,49 @@ def build(ref_root: str, fx: int) -> dict:
     return out
 
 
+def raw_dmi(ref_root: str, fx: int) -> dict:
+    """The single-subject DMI, its priors and its samples' shape as the S4
+    slots hold them (before flattening): what a .Call shim reads with the R
+    C API and hands to the converters of include/ggdmc_dmi.h."""
+    d = load_rda(os.path.join(ref_root, "tests/testthat/Group1/data", f"lba_data{fx}.rda"))
+    dmi = d["sub_dmis"][0]
+    m = dmi["model"]
+    mb = m["model_boolean"]
+    consts = m["constants"]
+    data = dmi["data"]
+    prior = d["sub_priors"]["p_prior"]
+    fields = [list(item.names) for item in prior.items]
+    values = [[float(v.data[0]) if len(v.data) else np.nan for v in item.items] for item in prior.items]
+    return {
+        "type": np.array(m["type"].data),
+        "model_boolean": np.asarray(mb.data, np.int32),          # column-major [ncell, npxc, K]
+        "model_boolean_dim": np.asarray(mb.attrs["dim"].data, np.int32),
+        "pxc_names": np.array(m["parameter_x_condition_names"].data),
+        "pnames": np.array(m["pnames"].data),
+        "constants": np.asarray(consts.data, np.float64),
+        "const_names": np.array(consts.attrs["names"].data),
+        "cell_names": np.array(m["cell_names"].data),
+        "accumulators": np.array(m["accumulators"].data),
+        "data_names": np.array(data.names),
+        "data_len": np.array([len(v.data) for v in data.items], np.int32),
+        "data_rt": np.concatenate([np.asarray(v.data, np.float64) for v in data.items]),
+        "prior_fields": np.array(fields),
+        "prior_values": np.array(values, np.float64),
+    }
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GGDMC_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set GGDMC_REFERENCE)")
     for fx in range(7):
         arrs = build(ref, fx)
         path = os.path.join(HERE, f"lba_fx{fx}.npz")
         np.savez_compressed(path, **arrs)
+        print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+    for fx in (3, 6):
+        path = os.path.join(HERE, f"dmi_raw_fx{fx}.npz")
+        np.savez_compressed(path, **raw_dmi(ref, fx))
         print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
 
