@@ -110,118 +110,237 @@ __device__ __forceinline__ double lba_logdens64(double t, const int *ents, int K
     return log(d);
 }
 
-// The winner's density in FP32.  When both normal arguments are >= 0 the
-// density is a sum of same-sign upper-tail terms, each relative-accurate in
-// FP32 (Mills-ratio tails), so a small density is exact enough; only one
-// within 0.1% of the reference's 1e-10 floor is re-evaluated (the floor
-// decision must agree), and one below is floored here.  Otherwise (a slow
-// response) the two terms cancel to leading order and a density below 1e-8
-// is re-evaluated in FP64.
-__device__ __forceinline__ bool winner_pdf_usable(bool fast, float &pdf)
+// ------------------------------------------------------ FP32 LBA trial
+// The trial density d = pdf_w(t) prod_{k != w} S_k(t) of the reference form
+// (lba_logdens64), evaluated in FP32 so that its log is within ~1e-7 of the
+// FP64 value per trial with a bias below 1e-8, so that sums over thousands of
+// trials stay within 1e-6 relative.  In terms of z = beta/t - kappa
+// (beta = b/s, kappa = v/s), cz at b and czm at b - A, h = (cz - czm)/2 =
+// A/(2 s t), m = (cz + czm)/2 and g = s/(A Phi(kappa)):
+//
+//   pdf_w = g * br,  br = kappa (Phi(cz) - Phi(czm)) + phi(czm) - phi(cz)
+//                       = integral over [czm, cz] of (z + kappa) phi(z)
+//   S_k   = 1 - g t int Q  (early, cz >= 0)  =  g t int Phi - q  (late, cz < 0)
+//         = avg Phi - q avg Q over [czm, cz],  q = Phi(-kappa)/Phi(kappa)
+//
+// Where the interval is narrow (h max(1, |m|) < 1/8: small A or slow
+// responses) the closed forms cancel, so the integrals are taken by 3-node
+// Gauss-Legendre quadrature about m, whose truncation error is below 2e-9
+// there.  Accuracy measures, each of which removed a measured bias:
+//  - t = RT - t0, u = 1/t and the z values are double-float (hi + lo), so
+//    exp(-z^2/2) keeps full accuracy out to the tails (its error is z dz);
+//  - every per-proposal constant is formed in FP64 and kept as a hi + lo pair
+//    where its rounding would scale all trials alike (beta, betam, kappa, hA,
+//    g, q); log g of the winner enters the sum in FP64, once per cell;
+//  - 1/sqrt(2 pi) is applied as a hi + lo pair, the Mills ratio's mean
+//    relative bias (-1.45e-8 over [0, 14]) is removed, the quadrature weights
+//    sum to 1 exactly;
+//  - the log is split: d = m 2^e, e summed as an integer, log m from the
+//    series 2 atanh((m-1)/(m+1)) on [sqrt(1/2), sqrt(2)).
+// A trial is left to the FP64 form (returns false) where FP32 cannot follow
+// the reference form: t < 1e-4; a winner bracket or survivor that cancels by
+// more than 16x; a pdf within 0.1% of the reference's 1e-10 floor (below it
+// the pdf is floored here); where the reference form's own FP64 rounding
+// exceeds 1e-8 relative (it differences Phi values near 1, or survivor terms
+// much larger than the survivor), so that the value follows the reference;
+// and a product outside the normal FP32 range.
+//
+// Per proposal and accumulator tuple (the host builds them in FP64):
+struct Ent32 {
+    float4 a;   // beta_h, betam_h, kappa_h, hA_h      hA = A / (2 s)
+    float4 b;   // beta_l, betam_l, kappa_l, hA_l      (low parts)
+    float4 c;   // g_h, g_l, q_h, q_l
+};
+
+constexpr float kPhiC = 0.398942280401432678f;            // 1/sqrt(2 pi), hi
+constexpr float kPhiCl = -1.13351701e-8f;                  // 1/sqrt(2 pi) - kPhiC
+constexpr float kGlX1 = 0.774596669241483f;                // sqrt(3/5)
+constexpr float kGlW1 = 0.277777791f;                      // 5/18 in FP32
+constexpr float kGlW0 = 0.444444418f;                      // 1 - 2 kGlW1, exactly
+constexpr float kGlMax = 0.125f;                           // h max(1,|m|) below: quadrature
+constexpr float kAmp = 16.f;                               // cancellation allowed
+constexpr float kMillsBias = 1.45e-8f;                     // mean relative bias removed
+constexpr double kLn2 = 0.693147180559945309417;
+
+// a - b as hi + lo (Knuth's two-sum)
+__device__ __forceinline__ void two_diff(float a, float b, float &s, float &e)
 {
-    if (!fast) return pdf >= 1e-8f;
-    if (pdf > 1.001e-10f) return true;
-    if (pdf < 0.999e-10f) {       // also 0 and underflowed tails
-        pdf = 1e-10f;
-        return true;
-    }
-    return false;                  // near the floor, or NaN
+    s = a - b;
+    const float bb = s - a;
+    e = (a - (s - bb)) - (b + bb);
 }
 
-// ------------------------------------------------------ FP32 LBA trial
-// e32a[u] = (beta = b/s, betam = (b-A)/s, kappa = v/s, cs = s/(A Phi(v/s)))
-// e32b[u] = (cv = v/(A Phi(v/s)), q = Phi(-v/s)/Phi(v/s))
-// z = beta/t - kappa.  Winner: pdf = cv*(Phi(cz)-Phi(czm)) + cs*(phi(czm)-phi(cz)),
-// with the difference taken on the upper tail when czm >= 0.  Loser survivor:
-// late (cz < 0) t*cs*(phi(cz)-phi(czm) + cz Phi(cz) - czm Phi(czm)) - q,
-// early 1 - t*cs*(cz Q(cz) - czm Q(czm) + phi(czm) - phi(cz)).
-// Returns false when the trial must be re-evaluated in FP64: a survivor in
-// the range where either form loses digits, a pdf near the 1e-10 floor, a
-// non-positive product or t below 1e-4 s.
-__device__ __forceinline__ bool lba_logdens32(float t, const uint8_t *ents, int K, int w,
-                                              const float4 *e32a, const float2 *e32b,
-                                              float &ld)
+// z = beta u - kappa in double-float (beta, u, kappa as hi + lo), normalised
+__device__ __forceinline__ void zdf(float bh, float bl, float uh, float ul, float kh, float kl,
+                                    float &zh, float &zl)
 {
-    if (!(t > 1e-4f)) return false;
-    const float it = __frcp_rn(t);
-    float pdf;
-    bool pdf_ok;
-    {
-        const float4 a = e32a[ents[w]];
-        const float2 b = e32b[ents[w]];
-        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
-        const float pz = phi32(cz), pm = phi32(czm);
-        const bool fast = czm >= 0.f;
-        const float sg = fast ? -1.f : 1.f;
-        const float d = sg * (ncdf32(sg * cz, pz) - ncdf32(sg * czm, pm));
-        pdf = fmaf(b.x, d, a.w * (pm - pz));
-        pdf_ok = winner_pdf_usable(fast, pdf);
+    const float p = bh * uh;
+    float pe = fmaf(bh, uh, -p);
+    pe = fmaf(bh, ul, pe);
+    pe = fmaf(bl, uh, pe);
+    float s, e;
+    two_diff(p, kh, s, e);
+    const float l = e + (pe - kl);
+    zh = s + l;
+    zl = l - (zh - s);
+}
+
+// phi(z) of a double-float z: exp(-zh^2/2) (1 - zh zl - (zh^2 - fl(zh^2))/2) / sqrt(2 pi)
+__device__ __forceinline__ float phidf(float zh, float zl)
+{
+    const float hh = zh * zh, hl = fmaf(zh, zh, -hh);
+    const float e0 = expf(-0.5f * hh);
+    const float e = fmaf(e0, kPhiC, e0 * kPhiCl);
+    return fmaf(e, fmaf(-zh, zl, -0.5f * hl), e);
+}
+
+// The normal tail beyond z (upper for z >= 0, lower for z < 0) from phi(z).
+__device__ __forceinline__ float ntail(float z, float ph)
+{
+    const float m = mills32(fabsf(z));
+    return ph * fmaf(m, kMillsBias, m);
+}
+
+// P = m 2^e with m in [sqrt(1/2), sqrt(2)); returns log m.  P > 0, normal.
+__device__ __forceinline__ float log_split(float P, int &e)
+{
+    const unsigned bits = __float_as_uint(P);
+    e = (int)(bits >> 23) - 127;
+    float m = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) {
+        m *= 0.5f;
+        ++e;
     }
-    float surv = 1.f;
-    bool bad = false;
-    for (int j = 0; j < K - 1; ++j) {
-        const int k = (j < w) ? j : j + 1;
-        const float4 a = e32a[ents[k]];
-        const float2 b = e32b[ents[k]];
-        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
-        const float pz = phi32(cz), pm = phi32(czm);
-        const bool late = cz < 0.f;
-        const float sg = late ? 1.f : -1.f;
-        const float br = fmaf(cz, ncdf32(sg * cz, pz), -czm * ncdf32(sg * czm, pm)) + sg * (pz - pm);
-        const float tcs = t * a.w;
-        const float S = late ? fmaf(tcs, br, -b.y) : fmaf(-tcs, br, 1.f);
-        surv *= S;
-        // Early, S = 1 - F cancels as F -> 1; late, S1/Phi(v/s) - q cancels as
-        // S1 -> Phi(-v/s); below 1e-9 the reference's own FP64 form loses its
-        // digits (it cancels to <= 0 and takes DBL_EPSILON), so follow it there.
-        bad |= late ? !(S >= 1e-9f && S * 32.f >= b.y) : !(S >= 1e-2f);
+    const float s = __fdividef(m - 1.f, m + 1.f), s2 = s * s;
+    const float poly = fmaf(fmaf(fmaf(fmaf(2.f / 11.f, s2, 2.f / 9.f), s2, 2.f / 7.f), s2, 2.f / 5.f), s2,
+                            2.f / 3.f);
+    return fmaf(s * s2, poly, 2.f * s);
+}
+
+// Winner bracket br (pdf = g br) of one accumulator; false: FP64 form.
+__device__ __forceinline__ bool winner_br(const Ent32 &P, float uh, float ul, float &br)
+{
+    float czh, czl, cmh, cml;
+    zdf(P.a.x, P.b.x, uh, ul, P.a.z, P.b.z, czh, czl);
+    zdf(P.a.y, P.b.y, uh, ul, P.a.z, P.b.z, cmh, cml);
+    const float h = P.a.w * uh, hc = fmaf(P.a.w, ul, P.b.w * uh);
+    const float mh = czh - h, ml = (czl - hc) + ((czh - mh) - h);
+    float ref;   // the reference form's FP64 rounding in its bracket
+    if (h * fmaxf(1.f, fabsf(mh)) < kGlMax) {
+        const float pm = phidf(mh, ml);
+        const float hx = h * kGlX1, a = hx * mh, c = 0.5f * hx * hx;
+        const float ep = expf(a - c), em = expf(-a - c);          // phi(m -/+ hx) / phi(m)
+        const float mk = (mh + P.a.z) + (ml + P.b.z);            // m + kappa
+        const float inner = fmaf(kGlW1, fmaf(mk + hx, em, (mk - hx) * ep), kGlW0 * mk);
+        const float y = 2.f * pm * inner, x2 = fmaf(y, uh, y * ul);
+        br = fmaf(P.a.w, x2, P.b.w * x2);
+        const float phimax = (mh < -1.f) ? pm / -mh : 1.f;       // Phi(m) <= phi(m) / |m|
+        ref = 1.1e-16f * (fabsf(P.a.z) * phimax + 2.f * pm);
+        if (!(br > 0.f)) return false;
+    } else {
+        const float pz = phidf(czh, czl), pm = phidf(cmh, cml);
+        const float tz = ntail(czh, pz), tm = ntail(cmh, pm);
+        const bool fast = cmh >= 0.f;
+        const float phimax = fast ? 1.f : ((czh < 0.f) ? tz : 1.f - tz);
+        const float dP = fast ? tm - tz : phimax - tm, dp = pm - pz;
+        br = fmaf(P.a.z, dP, fmaf(P.b.z, dP, dp));
+        ref = 1.1e-16f * (fabsf(P.a.z) * phimax + pm + pz);
+        if (!(br > 0.f) || !(br * kAmp >= fabsf(P.a.z * dP) + fabsf(dp))) return false;
     }
-    const float d = pdf * surv;
-    if (bad || !pdf_ok || !(d >= 1.2e-38f) || !(d < 3.0e38f)) return false;
-    ld = __logf(d);
+    const float pdf = br * P.c.x;
+    if (pdf < 0.999e-10f) {
+        br = __fdividef(1e-10f, P.c.x);     // the reference's floor
+        return true;
+    }
+    return pdf >= 1.001e-10f && br * 1e-8f >= ref;
+}
+
+// Survivor S of a losing accumulator; false: FP64 form.
+__device__ __forceinline__ bool loser_s(const Ent32 &P, float th, float tl, float uh, float ul, float &S)
+{
+    float czh, czl, cmh, cml;
+    zdf(P.a.x, P.b.x, uh, ul, P.a.z, P.b.z, czh, czl);
+    zdf(P.a.y, P.b.y, uh, ul, P.a.z, P.b.z, cmh, cml);
+    const float h = P.a.w * uh, hc = fmaf(P.a.w, ul, P.b.w * uh);
+    const float mh = czh - h, ml = (czl - hc) + ((czh - mh) - h);
+    float terms;   // the reference's survivor sums terms of this size, scaled 1/(2h)
+    bool ok;
+    if (h * fmaxf(1.f, fabsf(mh)) < kGlMax) {
+        const float p0 = phidf(mh, ml);
+        const float hx = h * kGlX1, a = hx * mh, c = 0.5f * hx * hx;
+        const float zp = mh + hx, zn = mh - hx;
+        const float pp = p0 * expf(-a - c), pn = p0 * expf(a - c);
+        const float t0 = ntail(mh, p0), tp = ntail(zp, pp), tn = ntail(zn, pn);
+        const float P0 = (mh < 0.f) ? t0 : 1.f - t0, Q0 = (mh < 0.f) ? 1.f - t0 : t0;
+        const float Pp = (zp < 0.f) ? tp : 1.f - tp, Qp = (zp < 0.f) ? 1.f - tp : tp;
+        const float Pn = (zn < 0.f) ? tn : 1.f - tn, Qn = (zn < 0.f) ? 1.f - tn : tn;
+        const float aP = fmaf(kGlW1, Pp + Pn, kGlW0 * P0), aQ = fmaf(kGlW1, Qp + Qn, kGlW0 * Q0);
+        const float qa = P.c.z * aQ;
+        S = fmaf(-P.c.z, aQ, aP) - P.c.w * aQ;
+        ok = S > 0.f && S * kAmp >= qa;
+        terms = 2.f * (fabsf(mh) * P0 + p0);
+    } else {
+        const float pz = phidf(czh, czl), pm = phidf(cmh, cml);
+        const float tz = ntail(czh, pz), tm = ntail(cmh, pm);
+        const bool late = czh < 0.f;
+        // late: both tails are lower tails (Phi); early: Q(cz) = tz, Q(czm) by its sign
+        const float Qm = (cmh < 0.f) ? 1.f - tm : tm;
+        const float iX = late ? fmaf(czh, tz, -cmh * tm) + (pz - pm) : fmaf(czh, tz, -cmh * Qm) + (pm - pz);
+        const float x = fmaf(th, iX, tl * iX);
+        S = late ? fmaf(P.c.x, x, -P.c.z) + fmaf(P.c.y, x, -P.c.w) : fmaf(-P.c.x, x, fmaf(-P.c.y, x, 1.f));
+        ok = late ? S * kAmp >= P.c.z : S >= 1.f / kAmp;
+        const float Pz = late ? tz : 1.f - tz, Pm = (cmh < 0.f) ? tm : 1.f - tm;
+        terms = fabsf(czh) * Pz + fabsf(cmh) * Pm + pm + pz;
+    }
+    const float ref = 1.1e-16f * (1.f + __fdividef(terms, 2.f * h)) * (1.f + P.c.z);
+    return ok && S * 1e-8f >= ref;
+}
+
+// Log density of one trial in FP32 for K accumulators, the cell's entry ids
+// winner first: d = g_w * (m 2^e); returns e and log m (the caller adds
+// log g_w in FP64).  rt, t0: (hi, lo) splits.  false: use the FP64 form.
+template <int K>
+__device__ __forceinline__ bool lba_ld32(float2 rt, float2 t0, const int (&ent)[K], const Ent32 *E, int &e,
+                                         float &lm)
+{
+    float th, te;
+    two_diff(rt.x, t0.x, th, te);
+    const float tl = te + (rt.y - t0.y);
+    if (!(th > 1e-4f)) return false;
+    const float uh = __frcp_rn(th);
+    const float ul = uh * fmaf(-tl, uh, fmaf(-th, uh, 1.f));
+    float P;
+    if (!winner_br(E[ent[0]], uh, ul, P)) return false;
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        float S;
+        if (!loser_s(E[ent[k]], th, tl, uh, ul, S)) return false;
+        P *= S;
+    }
+    if (!(P >= 1.2e-38f) || !(P < 3.0e38f)) return false;
+    lm = log_split(P, e);
     return true;
 }
 
-// lba_logdens32 for a fixed accumulator count, with the cell's entry ids in
-// registers, winner first (the host stores each cell's entries that way).
-template <int K>
-__device__ __forceinline__ bool lba_logdens32_k(float t, const int (&ent)[K], const float4 *e32a,
-                                                const float2 *e32b, float &ld)
+// The same for a run-time accumulator count (<= kMaxAcc): ents winner first.
+__device__ __forceinline__ bool lba_ld32_n(float2 rt, float2 t0, const uint8_t *ents, int K, const Ent32 *E,
+                                           int &e, float &lm)
 {
-    if (!(t > 1e-4f)) return false;
-    const float it = __frcp_rn(t);
-    float pdf;
-    bool pdf_ok;
-    {
-        const float4 a = e32a[ent[0]];
-        const float2 b = e32b[ent[0]];
-        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
-        const float pz = phi32(cz), pm = phi32(czm);
-        const bool fast = czm >= 0.f;
-        const float sg = fast ? -1.f : 1.f;
-        const float d = sg * (ncdf32(sg * cz, pz) - ncdf32(sg * czm, pm));
-        pdf = fmaf(b.x, d, a.w * (pm - pz));
-        pdf_ok = winner_pdf_usable(fast, pdf);
-    }
-    float surv = 1.f;
-    bool bad = false;
-#pragma unroll
+    float th, te;
+    two_diff(rt.x, t0.x, th, te);
+    const float tl = te + (rt.y - t0.y);
+    if (!(th > 1e-4f)) return false;
+    const float uh = __frcp_rn(th);
+    const float ul = uh * fmaf(-tl, uh, fmaf(-th, uh, 1.f));
+    float P;
+    if (!winner_br(E[ents[0]], uh, ul, P)) return false;
     for (int k = 1; k < K; ++k) {
-        const float4 a = e32a[ent[k]];
-        const float2 b = e32b[ent[k]];
-        const float cz = fmaf(a.x, it, -a.z), czm = fmaf(a.y, it, -a.z);
-        const float pz = phi32(cz), pm = phi32(czm);
-        const bool late = cz < 0.f;
-        const float sg = late ? 1.f : -1.f;
-        const float br = fmaf(cz, ncdf32(sg * cz, pz), -czm * ncdf32(sg * czm, pm)) + sg * (pz - pm);
-        const float tcs = t * a.w;
-        const float S = late ? fmaf(tcs, br, -b.y) : fmaf(-tcs, br, 1.f);
-        surv *= S;
-        bad |= late ? !(S >= 1e-9f && S * 32.f >= b.y) : !(S >= 1e-2f);
+        float S;
+        if (!loser_s(E[ents[k]], th, tl, uh, ul, S)) return false;
+        P *= S;
     }
-    const float d = pdf * surv;
-    if (bad || !pdf_ok || !(d >= 1.2e-38f) || !(d < 3.0e38f)) return false;
-    ld = __logf(d);
+    if (!(P >= 1.2e-38f) || !(P < 3.0e38f)) return false;
+    lm = log_split(P, e);
     return true;
 }
 

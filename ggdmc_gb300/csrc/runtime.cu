@@ -7,12 +7,12 @@
 // caller's arrays (R's posterior layout).
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
-#include <mutex>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -48,27 +48,17 @@ ggdmc_status fail(ggdmc_status s, const std::string &msg)
 constexpr size_t kScratchDoubles = (size_t)1 << 17;   // 1 MiB
 static __device__ __align__(256) double g_scratch[kScratchDoubles];
 
-constexpr size_t kMaxDevices = 64;
-std::mutex g_scratch_mu;
-double *g_scratch_ptr[kMaxDevices];
-
 size_t round256(size_t n_double) { return (n_double + 31) & ~(size_t)31; }
 
-// Device address of g_scratch on the current device, looked up once per
-// device (the lookup may load the module, so make the first call outside any
-// stream capture).
+// Device address of g_scratch in the current device's context, looked up on
+// every call (cheap once the module is loaded; a cached address would not
+// survive a device reset).  The first lookup on a device may load the module,
+// so make the first call outside any stream capture.
 ggdmc_status scratch_base(double **out)
 {
-    int dev = 0;
-    CU(cudaGetDevice(&dev));
-    if (dev < 0 || (size_t)dev >= kMaxDevices) return fail(GGDMC_ERR_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        CU(cudaGetSymbolAddress(&p, g_scratch));
-        g_scratch_ptr[dev] = static_cast<double *>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    CU(cudaGetSymbolAddress(&p, g_scratch));
+    *out = static_cast<double *>(p);
     return GGDMC_OK;
 }
 
@@ -190,13 +180,17 @@ struct ggdmc_handle {
     DevBuf<int32_t> partner, ptype, nstep, sub, migrated, ppartner, pptype, pnstep, psub,
         pmigrated, iter, status, items, items_plain, rs_para, sub_order, ready, spec_cnt, ctl;
     DevBuf<int8_t> need, pneed;
-    DevBuf<float4> tab_a;
-    DevBuf<float2> tab_b, tab_t;
+    DevBuf<Ent32> tab_e;
+    DevBuf<double> tab_lg;
+    DevBuf<float2> tab_t;
+    DevBuf<int32_t> cell_cnt;             // [S][n_cell] trials per subject and cell
     DevBuf<int32_t> tab_bad;
     DevBuf<double> jit, accu, pjit, paccu;
     DevBuf<double> smp_th, smp_lp, smp_ll, psmp_th, psmp_lp, psmp_ll, draws;
     DevBuf<unsigned long long> stats;
     DevBuf<double> io_a, io_b;
+    DevBuf<int32_t> ref_count, ref_base, ref_item;   // FP64 refinement of MIXED sums near zero
+    DevBuf<double> ref_partial;
     DevBuf<uint8_t> flushbuf;
     PinnedBuf stage[2];                   // sample chunks on their way to the caller's buffers
 
@@ -417,6 +411,12 @@ ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
     if (N > 0 && (!d->rt || !d->cell)) return fail(GGDMC_ERR_ARG, "rt / cell missing");
     std::vector<float2> r32(N);
     std::vector<uint16_t> c16(N);
+    std::vector<int32_t> cnt((size_t)std::max(S, 1) * h->n_cell, 0);
+    for (int s = 0; s < S; ++s)
+        for (int64_t i = offs[s]; i < offs[s + 1]; ++i) {
+            const int c = d->cell[i];
+            if (c >= 0 && c < h->n_cell) ++cnt[(size_t)s * h->n_cell + c];
+        }
     for (int64_t i = 0; i < N; ++i) {
         const double rt = d->rt[i];
         if (!std::isfinite(rt)) return fail(GGDMC_ERR_ARG, "non-finite RT in data");
@@ -433,6 +433,7 @@ ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
     CU(h->rt64.upload(d->rt, N, st));
     CU(h->rt32.upload(r32.data(), N, st));
     CU(h->cell.upload(c16.data(), N, st));
+    CU(h->cell_cnt.upload(cnt.data(), cnt.size(), st));
     return wait_stream(st);
 }
 
@@ -442,6 +443,8 @@ ggdmc_status check_cfg(const ggdmc_de_config *c)
     if (c->nchain <= 2) return fail(GGDMC_ERR_ARG, "Require three or more chains.");
     if (c->nchain > kMaxChain) return fail(GGDMC_ERR_ARG, "nchain above 1024");
     if (c->nmc < 1 || c->thin < 1) return fail(GGDMC_ERR_ARG, "nmc and thin must be >= 1");
+    if ((int64_t)(c->nmc - 1) * c->thin > INT32_MAX - 1)
+        return fail(GGDMC_ERR_ARG, "(nmc - 1) * thin iterations exceed the 32-bit iteration counter");
     if (c->nparameter < 1 || c->nparameter > kMaxTheta)
         return fail(GGDMC_ERR_ARG, "nparameter out of range");
     if (!(c->rp > 0.0) || !(c->gamma_precursor > 0.0))
@@ -541,8 +544,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         CU(h->jit.alloc((size_t)S * C * P));
         CU(h->accu.alloc((size_t)S * C));
         CU(h->rs_para.alloc(S));
-        CU(h->tab_a.alloc((size_t)S * CS * h->n_ent));
-        CU(h->tab_b.alloc((size_t)S * CS * h->n_ent));
+        CU(h->tab_e.alloc((size_t)S * CS * h->n_ent));
+        CU(h->tab_lg.alloc((size_t)S * CS * h->n_ent));
         CU(h->tab_t.alloc((size_t)S * CS * h->n_t0));
         CU(h->tab_bad.alloc((size_t)S * CS));
         CU(h->smp_th.alloc((size_t)S * nmc * C * P));
@@ -666,7 +669,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.partner = h->partner.p; r.need = h->need.p; r.ptype = h->ptype.p; r.nstep = h->nstep.p;
     r.sub = h->sub.p; r.migrated = h->migrated.p;
     r.jit = h->jit.p; r.accu = h->accu.p;
-    r.tab_a = h->tab_a.p; r.tab_b = h->tab_b.p; r.tab_t = h->tab_t.p; r.tab_bad = h->tab_bad.p;
+    r.tab_e = h->tab_e.p; r.tab_lg = h->tab_lg.p; r.tab_t = h->tab_t.p; r.tab_bad = h->tab_bad.p;
+    r.cell_cnt = h->cell_cnt.p;
     r.rs_para = h->rs_para.p; r.CS = CS;
     r.sub_order = h->sub_order.p;
     r.pjit = h->pjit.p; r.paccu = h->paccu.p;
@@ -689,6 +693,11 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.spec_cnt = fused ? h->spec_cnt.p : nullptr;
     r.ctl = fused ? h->ctl.p : nullptr;
     r.iter_end = (int32_t)n_iter;
+    // GGDMC_SPEC_IDLE_LIMIT: polls before an idle CTA of the fused schedule
+    // gives up waiting (default 2^21, about 2 s); the run then completes and
+    // returns GGDMC_ERR_TIMEOUT
+    r.spec_idle_limit = 1 << 21;
+    if (const char *il = std::getenv("GGDMC_SPEC_IDLE_LIMIT")) r.spec_idle_limit = std::max(0, std::atoi(il));
 
     int64_t launches_per_iter = 0;
     // One DE iteration (src/de.cpp:201-242 / 272-383) as a launch sequence.
@@ -1263,7 +1272,26 @@ static RunDev loglik_desc(ggdmc_handle *h, int prec)
     r.prec = (prec == GGDMC_MIXED) ? PREC_MIXED : PREC_FP64;
     r.m = h->dev_model();
     r.offs = h->offs.p; r.rt64 = h->rt64.p; r.rt32 = h->rt32.p; r.cell = h->cell.p;
+    r.cell_cnt = h->cell_cnt.p;
     return r;
+}
+
+// The batch likelihood on device buffers; MIXED sums near zero are then
+// recomputed in FP64 (launch_refine) so each sum is within 1e-6 relative.
+static ggdmc_status loglik_launch(ggdmc_handle *h, const double *d_theta, int n_theta, int precision,
+                                  double *d_out, cudaStream_t st)
+{
+    RunDev r = loglik_desc(h, precision);
+    CU(launch_loglik_batch(r, d_theta, n_theta, d_out, st));
+    if (precision != GGDMC_MIXED) return GGDMC_OK;
+    const size_t cap = refine_capacity(h->h_offs.data(), h->S, n_theta);
+    CU(h->ref_count.alloc(1));
+    CU(h->ref_base.alloc((size_t)h->S * n_theta));
+    CU(h->ref_item.alloc(std::max<size_t>(cap, 1)));
+    CU(h->ref_partial.alloc(std::max<size_t>(cap, 1)));
+    CU(launch_refine(r, d_theta, n_theta, d_out, h->ref_count.p, h->ref_base.p, h->ref_item.p, h->ref_partial.p,
+                     4 * h->n_sm, st));
+    return GGDMC_OK;
 }
 
 ggdmc_status ggdmc_loglik_device(ggdmc_handle *h, const double *d_theta, int32_t n_theta,
@@ -1271,9 +1299,7 @@ ggdmc_status ggdmc_loglik_device(ggdmc_handle *h, const double *d_theta, int32_t
 {
     if (!h || !d_theta || !d_out || n_theta < 1) return fail(GGDMC_ERR_ARG, "bad loglik arguments");
     if (h->S < 1) return fail(GGDMC_ERR_ARG, "handle has no subjects");
-    RunDev r = loglik_desc(h, precision);
-    CU(launch_loglik_batch(r, d_theta, n_theta, d_out, (cudaStream_t)stream));
-    return GGDMC_OK;
+    return loglik_launch(h, d_theta, n_theta, precision, d_out, (cudaStream_t)stream);
 }
 
 ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta, int32_t precision,
@@ -1284,8 +1310,8 @@ ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta,
     const size_t nt = (size_t)h->S * n_theta;
     CU(h->io_a.upload(theta, nt * h->n_par, h->stream));
     CU(h->io_b.alloc(nt));
-    RunDev r = loglik_desc(h, precision);
-    CU(launch_loglik_batch(r, h->io_a.p, n_theta, h->io_b.p, h->stream));
+    ggdmc_status s = loglik_launch(h, h->io_a.p, n_theta, precision, h->io_b.p, h->stream);
+    if (s) return s;
     CU(cudaMemcpyAsync(out, h->io_b.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, h->stream));
     return wait_stream(h->stream);
 }

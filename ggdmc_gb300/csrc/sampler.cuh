@@ -74,10 +74,11 @@ struct RunDev {
     const int32_t *sub_order;      // [S] subjects by trial count, largest first
     int32_t CS;                    // proposal slots per level: C speculative + C variants
     // FP32 tables of every proposal slot, built where the proposal is built
-    float4 *tab_a;                 // [S*CS][n_ent] (b/s, (b-A)/s, v/s, s/(A Phi(v/s)))
-    float2 *tab_b;                 // [S*CS][n_ent] (v/(A Phi(v/s)), Phi(-v/s)/Phi(v/s))
+    Ent32 *tab_e;                  // [S*CS][n_ent] FP32 trial constants (device_common.cuh)
+    double *tab_lg;                // [S*CS][n_ent] log g of each tuple
     float2 *tab_t;                 // [S*CS][n_t0]  t0 as (hi, lo)
     int32_t *tab_bad;              // [S*CS] 1: outside the FP32 form's domain
+    const int32_t *cell_cnt;       // [S][n_cell] trials of each subject in each cell
     const double *prior;           // [P][kPriorRow] fixed subject prior (nullptr in HB)
     const double *pp_bounds;       // [P][2] p_prior (lower, upper) for HB / phi level
     double *phi_tab;               // [C][P][3] (mu, 1/sigma, c) of phi chain (HB)
@@ -104,6 +105,7 @@ struct RunDev {
     int32_t *spec_cnt;             // [S] spec items of the level claimed so far
     int32_t *ctl;                  // [3] levels claimed / resolved this pass, events
     int32_t iter_end;              // last iteration of the run
+    int32_t spec_idle_limit;       // polls (~1 us each) an idle k_sub_step CTA waits before giving up
 
     unsigned long long *stats;     // [ST_N]
     int32_t *status;
@@ -128,6 +130,11 @@ cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_thet
                                 cudaStream_t st);
 cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *out,
                                  cudaStream_t st);
+// FP64 refinement of the MIXED sums out [S][n_theta] near zero (theta as given
+// to launch_loglik_batch); buffers sized by refine_capacity.
+size_t refine_capacity(const int64_t *h_offs, int S, int n_theta);
+cudaError_t launch_refine(const RunDev &r, const double *theta, int n_theta, double *out, int32_t *count,
+                          int32_t *base, int32_t *item, double *partial, int grid, cudaStream_t st);
 cudaError_t launch_init_draw(const double *rows, int P, int C, int level0, int n_level, const int32_t *attempt,
                              const uint8_t *done, uint64_t seed, double *theta, cudaStream_t st);
 cudaError_t launch_summary(const double *smp, int L, int nmc, int C, int P, int start, double *cs,

@@ -21,7 +21,6 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
-#include <cstdio>
 #include <cstdint>
 
 #include "sampler.cuh"
@@ -95,73 +94,6 @@ __device__ __forceinline__ void ff_add(float &h, float &l, float h2, float l2)
     e += l + l2;
     h = s + e;
     l = e - (h - s);
-}
-
-// Sum of (h + l) over the CTA, reduced in FP32 double-float; every thread
-// gets the double result.
-__device__ __forceinline__ double block_sum_ff(float h, float l, double *red)
-{
-    for (int o = 16; o > 0; o >>= 1) {
-        const float h2 = __shfl_down_sync(0xffffffffu, h, o);
-        const float l2 = __shfl_down_sync(0xffffffffu, l, o);
-        ff_add(h, l, h2, l2);
-    }
-    float *rf = (float *)red;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nw = (blockDim.x + 31) >> 5;
-    if (lane == 0) { rf[2 * wid] = h; rf[2 * wid + 1] = l; }
-    __syncthreads();
-    if (wid == 0) {
-        h = (lane < nw) ? rf[2 * lane] : 0.f;
-        l = (lane < nw) ? rf[2 * lane + 1] : 0.f;
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, h, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, l, o);
-            ff_add(h, l, h2, l2);
-        }
-        if (lane == 0) red[32] = (double)h + (double)l;
-    }
-    __syncthreads();
-    const double out = red[32];
-    __syncthreads();
-    return out;
-}
-
-// block_sum_ff of the group's ng (h, l) pairs at once: one exchange through
-// shared memory, warp g reducing pair g.  Every thread gets out[0..ng).
-template <int G>
-__device__ __forceinline__ void block_sum_ff_group(const float (&h)[G], const float (&l)[G], int ng,
-                                                   double *red, double *out)
-{
-    float *rf = (float *)red;                     // [G][32] (h, l) pairs
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-        if (g >= ng) break;
-        float hh = h[g], ll = l[g];
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
-            ff_add(hh, ll, h2, l2);
-        }
-        if (lane == 0) { rf[2 * (g * 32 + wid)] = hh; rf[2 * (g * 32 + wid) + 1] = ll; }
-    }
-    __syncthreads();
-    double *res = red + G * 32;
-    for (int g = wid; g < ng; g += nw) {
-        float hh = (lane < nw) ? rf[2 * (g * 32 + lane)] : 0.f;
-        float ll = (lane < nw) ? rf[2 * (g * 32 + lane) + 1] : 0.f;
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
-            ff_add(hh, ll, h2, l2);
-        }
-        if (lane == 0) res[g] = (double)hh + (double)ll;
-    }
-    __syncthreads();
-    for (int g = 0; g < ng; ++g) out[g] = res[g];
-    __syncthreads();
 }
 
 __device__ __forceinline__ double prior_term(const double *row, double x)
@@ -332,9 +264,9 @@ struct SubSmem {
     double *theta;   // [kGroup][kMaxTheta]
     double *e64;     // n_ent * 5
     double *t064;    // n_t0
-    double *red;     // 165: block reductions
-    float4 *e32a;    // [kGroup][n_ent]
-    float2 *e32b;    // [kGroup][n_ent]
+    double *red;     // kRedDoubles: block reductions
+    Ent32 *e32;      // [kGroup][n_ent] FP32 trial constants of each proposal
+    double *lg;      // [kGroup][n_ent] log g of each tuple (FP64)
     float2 *t032;    // [kGroup][n_t0]
     uint8_t *cent;   // n_cell * n_acc
     uint8_t *cw;     // n_cell
@@ -349,17 +281,20 @@ struct SubSmem {
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 constexpr int kFbCap = 1024;   // FP64 re-evaluations a block lists before re-scanning its trials
+// block reductions: block_sum (33) or a group of kGroup (double, float pair,
+// int) sums, 3 doubles per warp and proposal, plus the results
+constexpr int kRedDoubles = 33 + kGroup * 32 * 3 + kGroup;
 
-__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[15])
+__host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[16])
 {
     size_t o = 0;
     off[0] = o; o += sizeof(double) * kMaxTheta * kGroup;
     off[1] = o; o += sizeof(double) * 5 * m.n_ent;
     off[2] = o; o += sizeof(double) * m.n_t0;
-    off[3] = o; o += sizeof(double) * (33 + 4 * 32 + 4);   // block_sum / block_sum_ff_group
+    off[3] = o; o += sizeof(double) * kRedDoubles;
     o = align_up(o, 16);
-    off[4] = o; o += sizeof(float4) * m.n_ent * kGroup;
-    off[5] = o; o += sizeof(float2) * m.n_ent * kGroup;
+    off[4] = o; o += sizeof(Ent32) * m.n_ent * kGroup;
+    off[5] = o; o += sizeof(double) * m.n_ent * kGroup;
     off[6] = o; o += sizeof(float2) * m.n_t0 * kGroup;
     off[7] = o; o += (size_t)m.n_cell * m.n_acc;
     off[8] = o; o += m.n_cell;
@@ -377,21 +312,21 @@ __host__ __device__ inline size_t sub_smem_layout(const DevModel &m, size_t off[
 
 __host__ __device__ size_t sub_smem_bytes(const DevModel &m)
 {
-    size_t off[15];
+    size_t off[16];
     return sub_smem_layout(m, off);
 }
 
 __device__ SubSmem carve(char *base, const DevModel &m)
 {
-    size_t off[15];
+    size_t off[16];
     sub_smem_layout(m, off);
     SubSmem s;
     s.theta = (double *)(base + off[0]);
     s.e64 = (double *)(base + off[1]);
     s.t064 = (double *)(base + off[2]);
     s.red = (double *)(base + off[3]);
-    s.e32a = (float4 *)(base + off[4]);
-    s.e32b = (float2 *)(base + off[5]);
+    s.e32 = (Ent32 *)(base + off[4]);
+    s.lg = (double *)(base + off[5]);
     s.t032 = (float2 *)(base + off[6]);
     s.cent = (uint8_t *)(base + off[7]);
     s.cw = (uint8_t *)(base + off[8]);
@@ -430,25 +365,37 @@ __device__ void build_tables64(const RunDev &r, SubSmem &sm, const double *theta
         sm.t064[q] = src_value(r.m.t0_src[q], theta, r.m.consts);
 }
 
-// FP32 table entry u of theta.  The exponent-sensitive ratios b/s, (b-A)/s
-// and v/s are formed in FP64 and rounded once; the scale factors in FP32.
-// Returns false when the tuple is outside the FP32 form's domain.
-__device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, int u, float4 &a, float2 &bb)
+// FP32 trial constants of tuple u of theta (Ent32, device_common.cuh), each
+// formed in FP64 and split into hi + lo FP32 parts, and lg = log g.  Returns
+// false when the tuple is outside the FP32 form's domain.
+__device__ __forceinline__ void split_f(double x, float &h, float &l)
+{
+    h = (float)x;
+    l = (float)(x - (double)h);
+}
+
+__device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, int u, Ent32 &E, double &lg)
 {
     const EntSrc es = r.m.ent_src[u];
     const double A = src_value(es.A, theta, r.m.consts);
     const double B = src_value(es.B, theta, r.m.consts);
     const double v = src_value(es.v, theta, r.m.consts);
     const double s = src_value(es.s, theta, r.m.consts);
-    const double b = A + B;
     const double is = 1.0 / s;
-    const float kap = (float)(v * is);
-    const float den = normcdff(kap), qv = normcdff(-kap);
-    const float iad = 1.f / ((float)A * den);
-    a = make_float4((float)(b * is), (float)((b - A) * is), kap, (float)s * iad);
-    bb = make_float2((float)v * iad, qv / den);
-    return A > 0.0 && s > 0.0 && den > 1e-30f && isfinite(a.x) && isfinite(a.y) && isfinite(a.z) &&
-           isfinite(a.w) && isfinite(bb.x) && isfinite(bb.y);
+    const double kap = v * is;
+    // Phi(kappa) and Phi(-kappa) from one erfc, each with full relative accuracy
+    const double tl = 0.5 * erfc(fabs(kap) * 0.70710678118654752440);
+    const double den = (kap >= 0.0) ? 1.0 - tl : tl, qt = (kap >= 0.0) ? tl : 1.0 - tl;
+    const double g = s / (A * den), q = qt / den;
+    split_f((A + B) * is, E.a.x, E.b.x);
+    split_f(B * is, E.a.y, E.b.y);
+    split_f(kap, E.a.z, E.b.z);
+    split_f(0.5 * A * is, E.a.w, E.b.w);
+    split_f(g, E.c.x, E.c.y);
+    split_f(q, E.c.z, E.c.w);
+    lg = log(g);
+    return A > 0.0 && s > 0.0 && den > 1e-30 && isfinite(E.a.x) && isfinite(E.a.y) && isfinite(E.a.z) &&
+           isfinite(E.c.x) && isfinite(E.c.z) && E.a.w > 0.f && E.c.x > 0.f && isfinite(lg);
 }
 
 __device__ __forceinline__ float2 t0split(const RunDev &r, const double *theta, int q)
@@ -463,11 +410,11 @@ __device__ void build_tables32(const RunDev &r, SubSmem &sm, int g)
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0;
     for (int u = threadIdx.x; u < NE; u += blockDim.x) {
-        float4 a;
-        float2 bb;
-        if (!entry32(r, sm.theta + g * kMaxTheta, u, a, bb)) sm.flag[g] = 1;
-        sm.e32a[g * NE + u] = a;
-        sm.e32b[g * NE + u] = bb;
+        Ent32 E;
+        double lg;
+        if (!entry32(r, sm.theta + g * kMaxTheta, u, E, lg)) sm.flag[g] = 1;
+        sm.e32[g * NE + u] = E;
+        sm.lg[g * NE + u] = lg;
     }
     for (int q = threadIdx.x; q < NT; q += blockDim.x)
         sm.t032[g * NT + q] = t0split(r, sm.theta + g * kMaxTheta, q);
@@ -490,10 +437,11 @@ __device__ void load_slot(const RunDev &r, size_t slot, SubSmem &sm, int g, bool
     const int NE = r.m.n_ent, NT = r.m.n_t0;
     for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[g * kMaxTheta + j] = ldx<CO>(r.th_s + slot * r.P + j);
     if (!mixed) return;
-    for (int u = threadIdx.x; u < NE; u += blockDim.x) {
-        sm.e32a[g * NE + u] = ldx<CO>(r.tab_a + slot * NE + u);
-        sm.e32b[g * NE + u] = ldx<CO>(r.tab_b + slot * NE + u);
-    }
+    // the tables as float4 words: 3 per tuple
+    const float4 *src = reinterpret_cast<const float4 *>(r.tab_e + slot * NE);
+    float4 *dst = reinterpret_cast<float4 *>(sm.e32 + g * NE);
+    for (int u = threadIdx.x; u < 3 * NE; u += blockDim.x) dst[u] = ldx<CO>(src + u);
+    for (int u = threadIdx.x; u < NE; u += blockDim.x) sm.lg[g * NE + u] = ldx<CO>(r.tab_lg + slot * NE + u);
     for (int q = threadIdx.x; q < NT; q += blockDim.x) sm.t032[g * NT + q] = ldx<CO>(r.tab_t + slot * NT + q);
     if (threadIdx.x == 0) sm.flag[g] = ldx<CO>(r.tab_bad + slot);
 }
@@ -569,39 +517,116 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
     for (int g = 0; g < ng; ++g) out[g] = block_sum(acc[g] + ((double)ks[g] - (double)kc[g]), sm.red);
 }
 
+// Sums of a group of ng (<= G) proposals over the CTA, every thread gets
+// out[g] = sum d + sum (h - c) + ln 2 sum e: d the FP64 parts (the per-cell
+// log g constants and FP64 re-evaluations), h - c the Kahan-compensated FP32
+// sums of the mantissa logs (reduced as double-float pairs), e the binary
+// exponents (exact).  One exchange through shared memory, warp g reducing
+// proposal g; the order of every sum is fixed.
+template <int G>
+__device__ __forceinline__ void block_sum_mixed(const double (&d)[G], const float (&h)[G], const float (&c)[G],
+                                                const int (&e)[G], int ng, double *red, double *out)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    double *rd = red;                               // [G][32]
+    float *rf = (float *)(red + G * 32);            // [G][32] (h, l)
+    int *ri = (int *)(red + G * 64);                // [G][32]
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        if (g >= ng) break;
+        double dd = d[g];
+        float hh = h[g], ll = -c[g];
+        int ee = e[g];
+        for (int o = 16; o > 0; o >>= 1) {
+            dd += __shfl_down_sync(0xffffffffu, dd, o);
+            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
+            ff_add(hh, ll, h2, l2);
+            ee += __shfl_down_sync(0xffffffffu, ee, o);
+        }
+        if (lane == 0) {
+            rd[g * 32 + wid] = dd;
+            rf[2 * (g * 32 + wid)] = hh;
+            rf[2 * (g * 32 + wid) + 1] = ll;
+            ri[g * 32 + wid] = ee;
+        }
+    }
+    __syncthreads();
+    double *res = red + G * 96;
+    for (int g = wid; g < ng; g += nw) {
+        double dd = (lane < nw) ? rd[g * 32 + lane] : 0.0;
+        float hh = (lane < nw) ? rf[2 * (g * 32 + lane)] : 0.f;
+        float ll = (lane < nw) ? rf[2 * (g * 32 + lane) + 1] : 0.f;
+        int ee = (lane < nw) ? ri[g * 32 + lane] : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            dd += __shfl_down_sync(0xffffffffu, dd, o);
+            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
+            ff_add(hh, ll, h2, l2);
+            ee += __shfl_down_sync(0xffffffffu, ee, o);
+        }
+        if (lane == 0) res[g] = dd + ((double)hh + (double)ll) + kLn2 * (double)ee;
+    }
+    __syncthreads();
+    for (int g = 0; g < ng; ++g) out[g] = res[g];
+    __syncthreads();
+}
+
+// Kahan-compensated FP32 accumulation (sum s, compensation c)
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 // The FP32 pass of group_loglik over trials [base, base + n) for K
-// accumulators: each trial's entry ids are read once and shared by the
-// group's proposals.
+// accumulators (K = 0: the design's count at run time), one proposal at a
+// time, so a thread holds one proposal's sums; the subject's trial data is
+// read once per proposal (it stays in L1).  A trial the FP32 form declines
+// is listed for FP64.
 template <int K>
 __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, int n, const SubSmem &sm,
                                                  const bool (&ok)[kGroup], float (&ks)[kGroup],
-                                                 float (&kc)[kGroup], int (&nfb)[kGroup])
+                                                 float (&kc)[kGroup], int (&es)[kGroup], int (&nfb)[kGroup])
 {
-    const int NE = r.m.n_ent, NT = r.m.n_t0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int c = r.cell[base + i];
-        const float2 rt = r.rt32[base + i];
-        int ent[K];
+    const int NE = r.m.n_ent, NT = r.m.n_t0, KR = r.m.n_acc;
 #pragma unroll
-        for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
-        const int q0 = sm.ct0[c];
+    for (int g = 0; g < kGroup; ++g) {
+        if (!ok[g]) continue;                       // uniform over the block
+        const Ent32 *E = sm.e32 + g * NE;
+        const float2 *T0 = sm.t032 + g * NT;
+        float s = 0.f, cmp = 0.f;
+        int e = 0, nf = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int c = r.cell[base + i];
+            const float2 rt = r.rt32[base + i];
+            int ex;
+            float lm;
+            bool good;
+            if constexpr (K > 0) {
+                int ent[K];
 #pragma unroll
-        for (int g = 0; g < kGroup; ++g) {
-            if (!ok[g]) continue;
-            const float2 t0 = sm.t032[g * NT + q0];
-            const float t = (rt.x - t0.x) + (rt.y - t0.y);
-            float ld;
-            if (lba_logdens32_k<K>(t, ent, sm.e32a + g * NE, sm.e32b + g * NE, ld)) {
-                const float y = ld - kc[g];     // Kahan-compensated FP32 sum
-                const float tt = ks[g] + y;
-                kc[g] = (tt - ks[g]) - y;
-                ks[g] = tt;
+                for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
+                good = lba_ld32<K>(rt, T0[sm.ct0[c]], ent, E, ex, lm);
             } else {
-                ++nfb[g];
+                good = lba_ld32_n(rt, T0[sm.ct0[c]], sm.cent + c * KR, KR, E, ex, lm);
+            }
+            if (good) {
+                kahan_add(s, cmp, lm);
+                e += ex;
+            } else {
+                ++nf;
                 const int pos = atomicAdd(sm.fbn, 1);
                 if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
             }
         }
+        ks[g] = s;
+        kc[g] = cmp;
+        es[g] = e;
+        nfb[g] = nf;
     }
 }
 
@@ -610,22 +635,27 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
 // kLba4 only the 4-accumulator LBA loop.
 constexpr int kAnyModel = 0, kLbaOnly = 1, kDdmOnly = 2, kLba4 = 3;
 
+// Log-likelihood sums of the subject's trials for the ng (<= kGroup)
+// proposals loaded in sm, on the whole CTA; out[g] valid on all threads.
+// MIXED: a trial's log density is log g_w (in FP64, once per cell through
+// the subject's cell counts) + e ln 2 + log m from lba_ld32; FP64 tables are
+// built only for a proposal some trial of which needs the FP64 form, and only
+// those trials use it.
 template <int MODEL = kAnyModel>
-__device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed,
-                             double *out)
+__device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool mixed, double *out)
 {
+    const int64_t base = r.offs[l];
+    const int n = (int)(r.offs[l + 1] - base);
     if constexpr (MODEL == kDdmOnly) {
-        ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, out);
+        ddm_group_loglik(r, l, 0, n, sm, ng, mixed, out);
         return;
     }
     if constexpr (MODEL == kAnyModel) {
         if (r.m.model_type == kModelDdm) {
-            ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, out);
+            ddm_group_loglik(r, l, 0, n, sm, ng, mixed, out);
             return;
         }
     }
-    const int64_t base = r.offs[l] + i0;
-    const int n = i1 - i0;
     const int K = r.m.n_acc;
     const int NE = r.m.n_ent, NT = r.m.n_t0;
     if (!mixed) {
@@ -642,93 +672,73 @@ __device__ void group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm
     __syncthreads();
     bool ok[kGroup];
     float ks[kGroup], kc[kGroup];
-    int nfb[kGroup];
+    int es[kGroup], nfb[kGroup];
+    double d[kGroup];
 #pragma unroll
     for (int g = 0; g < kGroup; ++g) {
         ok[g] = g < ng && sm.flag[g] == 0;
-        ks[g] = 0.f; kc[g] = 0.f; nfb[g] = 0;
+        ks[g] = 0.f; kc[g] = 0.f; es[g] = 0; nfb[g] = 0; d[g] = 0.0;
     }
     switch (MODEL == kLba4 ? 4 : K) {
-    case 2: if constexpr (MODEL != kLba4) lba_group_loop32<2>(r, base, n, sm, ok, ks, kc, nfb); break;
-    case 3: if constexpr (MODEL != kLba4) lba_group_loop32<3>(r, base, n, sm, ok, ks, kc, nfb); break;
-    case 4: lba_group_loop32<4>(r, base, n, sm, ok, ks, kc, nfb); break;
-    default:
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int c = r.cell[base + i];
-            const float2 rt = r.rt32[base + i];
-            const uint8_t *ents = sm.cent + c * K;
-            const int w = sm.cw[c], q0 = sm.ct0[c];
-#pragma unroll
-            for (int g = 0; g < kGroup; ++g) {
-                if (!ok[g]) continue;
-                const float2 t0 = sm.t032[g * NT + q0];
-                const float t = (rt.x - t0.x) + (rt.y - t0.y);
-                float ld;
-                if (lba_logdens32(t, ents, K, w, sm.e32a + g * NE, sm.e32b + g * NE, ld)) {
-                    const float y = ld - kc[g];     // Kahan-compensated FP32 sum
-                    const float tt = ks[g] + y;
-                    kc[g] = (tt - ks[g]) - y;
-                    ks[g] = tt;
-                } else {
-                    ++nfb[g];
-                    const int pos = atomicAdd(sm.fbn, 1);
-                    if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
-                }
-            }
-        }
+    case 2: if constexpr (MODEL != kLba4) lba_group_loop32<2>(r, base, n, sm, ok, ks, kc, es, nfb); break;
+    case 3: if constexpr (MODEL != kLba4) lba_group_loop32<3>(r, base, n, sm, ok, ks, kc, es, nfb); break;
+    case 4: lba_group_loop32<4>(r, base, n, sm, ok, ks, kc, es, nfb); break;
+    default: if constexpr (MODEL != kLba4) lba_group_loop32<0>(r, base, n, sm, ok, ks, kc, es, nfb); break;
     }
-    // no FP64 work anywhere in the group: one fused reduction
+    // log g of each trial's winning tuple, by cell: sum over cells of n_c log g
+    const int32_t *cnt = r.cell_cnt + (size_t)l * r.m.n_cell;
+    for (int c = threadIdx.x; c < r.m.n_cell; c += blockDim.x) {
+        const int nc = cnt[c];
+        if (!nc) continue;
+        const int u = sm.cent[c * K];
+#pragma unroll
+        for (int g = 0; g < kGroup; ++g)
+            if (ok[g]) d[g] += (double)nc * sm.lg[g * NE + u];
+    }
     bool anyfb = false;
 #pragma unroll
     for (int g = 0; g < kGroup; ++g)
         if (g < ng) anyfb |= nfb[g] > 0 || sm.flag[g] != 0;
-    if (!__syncthreads_or(anyfb)) {
-        float nkc[kGroup];
+    if (__syncthreads_or(anyfb)) {
+        // FP64 for the listed trials (their log g was counted above, so it
+        // is taken back out), or for every trial of a proposal outside the
+        // FP32 form's domain
 #pragma unroll
-        for (int g = 0; g < kGroup; ++g) nkc[g] = -kc[g];
-        block_sum_ff_group(ks, nkc, ng, sm.red, out);
-        return;
-    }
-#pragma unroll
-    for (int g = 0; g < kGroup; ++g) {
-        if (g >= ng) break;
-        const bool usable = sm.flag[g] == 0;
-        if (!__syncthreads_or(nfb[g] > 0 || !usable)) {
-            out[g] = block_sum_ff(ks[g], -kc[g], sm.red);
-            continue;
-        }
-        build_tables64(r, sm, sm.theta + g * kMaxTheta);
-        if (r.stats) {
-            const int nf = usable ? nfb[g] : (threadIdx.x == 0 ? n : 0);
-            if (nf) atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)nf);
-        }
-        __syncthreads();
-        double acc = usable ? (double)ks[g] - (double)kc[g] : 0.0;
-        const int fbn = *sm.fbn;
-        if (usable && fbn <= kFbCap) {
-            // only the listed trials of proposal g
-            for (int q = threadIdx.x; q < fbn; q += blockDim.x) {
-                const int e = sm.fb[q];
-                if ((e & 3) != g) continue;
-                const int i = e >> 2;
-                acc += trial64(r, sm, base + i, r.cell[base + i], K);
+        for (int g = 0; g < kGroup; ++g) {
+            if (g >= ng) break;
+            const bool usable = sm.flag[g] == 0;
+            if (!__syncthreads_or(nfb[g] > 0 || !usable)) continue;
+            build_tables64(r, sm, sm.theta + g * kMaxTheta);
+            if (r.stats) {
+                const int nf = usable ? nfb[g] : (threadIdx.x == 0 ? n : 0);
+                if (nf) atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)nf);
             }
-        } else if (!usable || nfb[g] > 0) {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const int c = r.cell[base + i];
-                if (usable) {
-                    const float2 rt = r.rt32[base + i];
-                    const float2 t0 = sm.t032[g * NT + sm.ct0[c]];
-                    const float t = (rt.x - t0.x) + (rt.y - t0.y);
-                    float ld;
-                    if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a + g * NE, sm.e32b + g * NE, ld))
-                        continue;
+            __syncthreads();
+            const int fbn = *sm.fbn;
+            if (!usable) {
+                for (int i = threadIdx.x; i < n; i += blockDim.x) d[g] += trial64(r, sm, base + i, r.cell[base + i], K);
+            } else if (fbn <= kFbCap) {
+                for (int q = threadIdx.x; q < fbn; q += blockDim.x) {
+                    const int e = sm.fb[q];
+                    if ((e & 3) != g) continue;
+                    const int i = e >> 2, c = r.cell[base + i];
+                    d[g] += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
                 }
-                acc += trial64(r, sm, base + i, c, K);
+            } else if (nfb[g] > 0) {
+                for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                    const int c = r.cell[base + i];
+                    int ex;
+                    float lm;
+                    if (lba_ld32_n(r.rt32[base + i], sm.t032[g * NT + sm.ct0[c]], sm.cent + c * K, K, sm.e32 + g * NE,
+                                   ex, lm))
+                        continue;
+                    d[g] += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
+                }
             }
+            __syncthreads();
         }
-        out[g] = block_sum(acc, sm.red);
     }
+    block_sum_mixed(d, ks, kc, es, ng, sm.red, out);
 }
 
 // Evaluate the log-likelihoods of proposal slots `slots[0..m)` of level l on
@@ -743,7 +753,7 @@ __device__ void eval_slots(const RunDev &r, int l, const int *slots, int m, SubS
         for (int g = 0; g < ng; ++g) load_slot<CO>(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
         __syncthreads();
         double out[kGroup];
-        group_loglik<MODEL>(r, l, 0, N, sm, ng, mixed, out);
+        group_loglik<MODEL>(r, l, sm, ng, mixed, out);
         if (threadIdx.x == 0) {
             for (int g = 0; g < ng; ++g) {
                 r.ll_s[(size_t)l * r.CS + slots[g0 + g]] = out[g];
@@ -761,11 +771,11 @@ __device__ __forceinline__ void store_entry(const RunDev &r, size_t slot, const 
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0;
     if (u < NE) {
-        float4 a;
-        float2 bb;
-        if (!entry32(r, theta, u, a, bb)) atomicOr(&r.tab_bad[slot], 1);
-        r.tab_a[slot * NE + u] = a;
-        r.tab_b[slot * NE + u] = bb;
+        Ent32 E;
+        double lg;
+        if (!entry32(r, theta, u, E, lg)) atomicOr(&r.tab_bad[slot], 1);
+        r.tab_e[slot * NE + u] = E;
+        r.tab_lg[slot * NE + u] = lg;
     } else {
         r.tab_t[slot * NT + (u - NE)] = t0split(r, theta, u - NE);
     }
@@ -1092,7 +1102,7 @@ __device__ void eval_direct(const RunDev &r, int l, const int *slots, int m, Sub
         for (int g = 0; g < ng; ++g) load_slot(r, (size_t)l * r.CS + slots[g0 + g], sm, g, mixed);
         __syncthreads();
         double o[kGroup];
-        group_loglik(r, l, 0, N, sm, ng, mixed, o);
+        group_loglik(r, l, sm, ng, mixed, o);
         if (threadIdx.x == 0) {
             for (int g = 0; g < ng; ++g) {
                 out[slots[g0 + g] - out_off] = o[g];
@@ -1308,18 +1318,9 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
     const int ct = threadIdx.x, cstride = blockDim.x;
     int rounds = 0, reevals = 0, variants = 0;
     int decided = 0;
-#ifdef GGDMC_PHASE_PROFILE
-    long long c_dec = 0, c_rep = 0, c_ev = 0, t_a = 0, t_start = clock64();
-#define PH_T0() t_a = clock64()
-#define PH_ADD(x) x += clock64() - t_a
-#else
-#define PH_T0()
-#define PH_ADD(x)
-#endif
     if (type == PASS_CROSS) {
         while (decided < n) {
             ++rounds;
-            PH_T0();
             // Metropolis outcome of every undecided step: it depends only on
             // the step's own proposal and its own chain's current state.
             for (int k = decided + threadIdx.x; k < n; k += blockDim.x)
@@ -1341,9 +1342,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             __syncthreads();
             write_accepts(r, l, type, n, rs, na);
             decided = d;
-            PH_ADD(c_dec);
             if (decided >= n) break;
-            PH_T0();
             // stale chains: a partner in [ver, decided) moved
             const int m = block_compact(decided, n, [&](int k) {
                 const int a = rs.pa[k], b = rs.pb[k], v = rs.ver[k];
@@ -1393,10 +1392,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                 for (int q = threadIdx.x; q < e; q += blockDim.x) rs.list[q] = rs.accslot[q];
                 __syncthreads();
             }
-            PH_ADD(c_rep);
-            PH_T0();
             eval_direct(r, l, rs.list, e, sm, mixed, rs.lls, 0);
-            PH_ADD(c_ev);
         }
     } else {
         // migration: cur[s] = log posterior of step s's destination, which
@@ -1421,7 +1417,6 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
         __syncthreads();
         while (decided < n) {
             ++rounds;
-            PH_T0();
             const int d = decided;
             // Round d > 0 starts because step d-1 was accepted, so step d's
             // source moved.  The value step s needs is fixed by the last
@@ -1509,15 +1504,11 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                 __syncthreads();
                 const int ne = rs.misc[3];
                 variants += ne;
-                PH_ADD(c_rep);
-                PH_T0();
                 if (ne) eval_direct(r, l, rs.list, ne, sm, mixed, rs.vll, C);
                 for (int w = threadIdx.x; w < nv; w += blockDim.x)
                     rs.vdec[w] = mh_accept((rs.vlp[w] + rs.vll[w]) - rs.cur[rs.vs[w]], rs.accu[rs.vs[w]]) ? 1 : 0;
                 __syncthreads();
             }
-            PH_ADD(c_ev);
-            PH_T0();
             if (threadIdx.x == 0) {
                 // the steps in order, each with the outcome of the value it
                 // needs, until one needs a value not evaluated yet
@@ -1558,15 +1549,8 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             decided = rs.misc[0];
             write_accepts(r, l, type, n, rs, rs.misc[1]);
             __syncthreads();
-            PH_ADD(c_dec);
         }
     }
-#ifdef GGDMC_PHASE_PROFILE
-    if (threadIdx.x == 0 && *r.iter == 3)
-        printf("PHASE l=%d type=%d N=%d n=%d reevals=%d variants=%d rounds=%d dec=%lld rep=%lld ev=%lld tot=%lld\n",
-               l, type, (int)(r.offs[l + 1] - r.offs[l]), n, reevals, variants, rounds, c_dec, c_rep, c_ev,
-               clock64() - t_start);
-#endif
     if (threadIdx.x == 0) {
         atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
         atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
@@ -1648,8 +1632,7 @@ k_sub_resolve(RunDev r, int level_begin, int n_level, int ordered, int score_pri
 // k_sub_spec_rest, which runs beside the phi level of t + 1.  An idle CTA
 // polls one event counter (bumped by every publication and every resolved
 // level); its waits are only for levels a running CTA holds, and bounded.
-constexpr int kSpecIdleLimit = 1 << 21;     // idle polls (~1 us each)
-constexpr int kStatusSpecWait = 3;
+constexpr int kStatusSpecWait = 3;           // RunDev::status when an idle wait gave up
 
 __device__ __forceinline__ int vload(const int32_t *p) { return *(const volatile int32_t *)p; }
 
@@ -1702,7 +1685,7 @@ k_sub_step(RunDev r, int score_priors, int defer_next, int group)
             for (int idle = 0;; ++idle) {
                 if (vload(r.ctl + kCtlResDone) >= r.S) { st = 0; break; }
                 if (vload(r.ctl + kCtlEvents) != seen) break;
-                if (idle > kSpecIdleLimit) {
+                if (idle > r.spec_idle_limit) {
                     atomicExch(r.status, kStatusSpecWait);
                     st = 2;
                     break;
@@ -2009,10 +1992,6 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
     if (r.phi_loop == LOOP_HCHAINS) para = r.phi_blocked ? pass : -1;
     else para = (type == PASS_MIG) ? -1 : (r.phi_blocked ? pass : -1);
     int reevals = 0, accepts = 0;
-#ifdef GGDMC_PHASE_PROFILE
-    long long c_dec = 0, c_rep = 0, c_ev = 0, t_a = 0, t_start = clock64();
-    int nround = 0;
-#endif
     if (type == PASS_CROSS) {
         for (int k = threadIdx.x; k < C; k += blockDim.x) {
             s_pa[k] = (int16_t)r.ppartner[2 * k];
@@ -2027,10 +2006,6 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
         __syncthreads();
         int decided = 0;
         while (decided < n) {
-#ifdef GGDMC_PHASE_PROFILE
-            ++nround;
-            t_a = clock64();
-#endif
             for (int k = decided + threadIdx.x; k < n; k += blockDim.x)
                 s_dec[k] = mh_accept((s_lps[k] + s_lls[k]) - (s_ref[k] + r.plp[k]), r.paccu[k]) ? 1 : 0;
             __syncthreads();
@@ -2060,10 +2035,6 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
             }
             decided = d;
             __syncthreads();
-#ifdef GGDMC_PHASE_PROFILE
-            c_dec += clock64() - t_a;
-            t_a = clock64();
-#endif
             if (decided >= n) break;
             if (threadIdx.x == 0) {
                 int m = 0;
@@ -2097,10 +2068,6 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
                 }
             }
             __syncthreads();
-#ifdef GGDMC_PHASE_PROFILE
-            c_rep += clock64() - t_a;
-            t_a = clock64();
-#endif
             for (int q0 = 0; q0 < m; q0 += kPhiBatch) {
                 const int mb = min(kPhiBatch, m - q0);
                 if (threadIdx.x < mb) {
@@ -2122,15 +2089,7 @@ __global__ void __launch_bounds__(kPhiResolveThreads) k_phi_resolve(RunDev r, in
                 r.pll_s[k] = s_lls[k];
             }
             __syncthreads();
-#ifdef GGDMC_PHASE_PROFILE
-            c_ev += clock64() - t_a;
-#endif
         }
-#ifdef GGDMC_PHASE_PROFILE
-        if (threadIdx.x == 0)
-            printf("PHIPHASE it=%d n=%d rounds=%d reevals=%d accepts=%d dec=%lld rep=%lld ev=%lld tot=%lld\n",
-                   (int)*r.iter, n, nround, reevals, accepts, c_dec, c_rep, c_ev, clock64() - t_start);
-#endif
     } else {
         // migration (pop_migration_prob per sweep): steps in order; a step
         // whose source was replaced by the previous step's accept is
@@ -2261,8 +2220,84 @@ __global__ void __launch_bounds__(kLikThreads, MINB) k_loglik_batch(RunDev r, co
     const bool mixed = r.prec == PREC_MIXED;
     if (mixed) build_tables32(r, sm, 0);
     double ll[kGroup];
-    group_loglik<MODEL>(r, l, 0, (int)(r.offs[l + 1] - r.offs[l]), sm, 1, mixed, ll);
+    group_loglik<MODEL>(r, l, sm, 1, mixed, ll);
     if (threadIdx.x == 0) out[(size_t)l * n_theta + k] = ll[0];
+}
+
+// ------------------------------------- FP64 refinement of sums near zero
+// The FP32 form's error in a sum of N trial log densities is a random walk of
+// about 1.5e-7 per trial plus a bias below 3e-8 per trial.  A sum whose size
+// is below kRefSig sqrt(N) + kRefBias N could therefore be off by more than
+// 1e-6 of itself; those sums are recomputed in FP64 (the reference form).
+// Their trials are split into chunks of kRefChunk, claimed by a grid-stride
+// loop over the whole GPU (a few sums of a few thousand trials would
+// otherwise occupy a few SMs for their FP64 work), and each sum is the
+// chunks' partial sums added in chunk order.
+constexpr int kRefChunk = 256;
+constexpr double kRefSig = 1.2, kRefBias = 0.03;
+
+// one thread per (subject, theta) sum: claim its chunks, or base = -1
+__global__ void k_refine_flag(RunDev r, const double *out, int n_theta, int32_t *count, int32_t *base,
+                              int32_t *item)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= r.S * n_theta) return;
+    const int l = q / n_theta;
+    const int n = (int)(r.offs[l + 1] - r.offs[l]);
+    const double T = kRefSig * sqrt((double)n) + kRefBias * n;
+    int b = -1;
+    if (n > 0 && !(fabs(out[q]) >= T)) {
+        const int nc = (n + kRefChunk - 1) / kRefChunk;
+        b = atomicAdd(count, nc);
+        for (int c = 0; c < nc; ++c) item[b + c] = q;
+    }
+    base[q] = b;
+}
+
+// chunks of the claimed sums in FP64, grid-stride
+__global__ void __launch_bounds__(kLikThreads) k_refine_eval(RunDev r, const double *theta, int n_theta,
+                                                             const int32_t *count, const int32_t *base,
+                                                             const int32_t *item, double *partial)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    SubSmem sm = carve(smem_raw, r.m);
+    load_design(r, sm);
+    const int nw = *count;
+    const int K = r.m.n_acc;
+    const bool ddm = r.m.model_type == kModelDdm;
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+        const int q = item[w], c = w - base[q];
+        const int l = q / n_theta;
+        __syncthreads();                    // the previous item's tables are no longer read
+        for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = theta[(size_t)q * r.P + j];
+        __syncthreads();
+        if (ddm) ddm_build(r, sm, 0, sm.theta);
+        else build_tables64(r, sm, sm.theta);
+        __syncthreads();
+        const int64_t b0 = r.offs[l];
+        const int n = (int)(r.offs[l + 1] - b0);
+        const int i1 = min(n, (c + 1) * kRefChunk);
+        double acc = 0.0;
+        for (int i = c * kRefChunk + threadIdx.x; i < i1; i += blockDim.x) {
+            const int cell = r.cell[b0 + i];
+            acc += ddm ? ddm_logdens64(r.rt64[b0 + i], sm.d64 + 8 * sm.cent[cell * K])
+                       : trial64(r, sm, b0 + i, cell, K);
+        }
+        const double s = block_sum(acc, sm.red);
+        if (threadIdx.x == 0) partial[w] = s;
+    }
+}
+
+// one thread per sum: the claimed sums' chunks added in order
+__global__ void k_refine_sum(RunDev r, int n_theta, const int32_t *base, const double *partial, double *out)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= r.S * n_theta || base[q] < 0) return;
+    const int l = q / n_theta;
+    const int nc = ((int)(r.offs[l + 1] - r.offs[l]) + kRefChunk - 1) / kRefChunk;
+    double s = 0.0;
+    for (int c = 0; c < nc; ++c) s += partial[base[q] + c];
+    out[q] = s;
 }
 
 // per-trial log densities of theta [S][P] -> out [N]; grid = S.
@@ -2300,12 +2335,10 @@ __global__ void __launch_bounds__(kLikThreads) k_trial_logdens(RunDev r, const d
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int c = r.cell[base + i];
         if (use32) {
-            const float2 rt = r.rt32[base + i];
-            const float2 t0 = sm.t032[sm.ct0[c]];
-            const float t = (rt.x - t0.x) + (rt.y - t0.y);
-            float ld;
-            if (lba_logdens32(t, sm.cent + c * K, K, sm.cw[c], sm.e32a, sm.e32b, ld)) {
-                out[base + i] = ld;
+            int ex;
+            float lm;
+            if (lba_ld32_n(r.rt32[base + i], sm.t032[sm.ct0[c]], sm.cent + c * K, K, sm.e32, ex, lm)) {
+                out[base + i] = sm.lg[sm.cent[c * K]] + kLn2 * (double)ex + (double)lm;
                 continue;
             }
         }
@@ -2405,6 +2438,7 @@ cudaError_t configure_kernels(const DevModel &m)
     if ((e = cudaFuncSetAttribute(k_loglik_batch<GGDMC_LIK_MINB, kDdmOnly>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
+    if ((e = cudaFuncSetAttribute(k_refine_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
     return cudaFuncSetAttribute(k_trial_logdens, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
@@ -2530,6 +2564,27 @@ cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_thet
         k_loglik_batch<GGDMC_LIK_MINB_LBA, kLba4><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out);
     else
         k_loglik_batch<GGDMC_LIK_MINB, kLbaOnly><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out);
+    return cudaGetLastError();
+}
+
+size_t refine_capacity(const int64_t *h_offs, int S, int n_theta)
+{
+    size_t n = 0;
+    for (int l = 0; l < S; ++l) n += (size_t)n_theta * (size_t)((h_offs[l + 1] - h_offs[l] + kRefChunk - 1) / kRefChunk);
+    return n;
+}
+
+cudaError_t launch_refine(const RunDev &r, const double *theta, int n_theta, double *out, int32_t *count,
+                          int32_t *base, int32_t *item, double *partial, int grid, cudaStream_t st)
+{
+    const int nq = r.S * n_theta;
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
+    if (e) return e;
+    k_refine_flag<<<(nq + 255) / 256, 256, 0, st>>>(r, out, n_theta, count, base, item);
+    if ((e = cudaGetLastError())) return e;
+    k_refine_eval<<<grid, kLikThreads, sub_smem_bytes(r.m), st>>>(r, theta, n_theta, count, base, item, partial);
+    if ((e = cudaGetLastError())) return e;
+    k_refine_sum<<<(nq + 255) / 256, 256, 0, st>>>(r, n_theta, base, partial, out);
     return cudaGetLastError();
 }
 
