@@ -114,23 +114,13 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def single_lba(seed: int = 0, n: int = 768):
-    """One subject of the 13-parameter design, 768 trials, U(0, 10) priors,
-    39 chains: the single-subject configuration."""
-    from ggdmc_gb300.design import BV13_POP_MEAN, design_bv13, vector
-    from ggdmc_gb300.dmi import SubjectBatch
-    rng = np.random.default_rng(seed)
-    model = design_bv13()
-    th = vector(model, BV13_POP_MEAN)
-    sub = synth.simulate_subject(model, th, n, rng, "1")
-    return synth.Workload("single_lba_768", model, SubjectBatch.pack([sub]), th[None],
-                          synth.unif_prior(model.n_par), None, None, None, 3 * model.n_par, False)
-
+FX6 = os.path.join(ROOT, "tests", "golden", "lba_fx6.npz")
 
 WORKLOADS = {
     "uneven_lba_256": synth.uneven_lba_256,
-    "single_lba_768": single_lba,
-    "hier_lba_32": synth.hier_lba_32,
+    # the reference fixture lba_data6.rda's own data and start samples
+    "single_lba_768": lambda: synth.fixture_lba_768(FX6, hierarchical=False),
+    "hier_lba_32": lambda: synth.fixture_lba_768(FX6, hierarchical=True),
     "hier_ddm_64": synth.hier_ddm_64,
     "many_fits_1024": synth.many_fits_1024,
 }
@@ -212,19 +202,27 @@ def loglik_roofline(w, h, n_launch=10):
     return ms, evals
 
 
-def cpu_baseline(w, n_sweeps=1, threads=None):
-    """The oracle on the host cores: `threads` replicas, each n_sweeps sweeps
-    of the full workload (FP64, reference chain order)."""
-    from oracle import binding as ob
-    ob.build()
+def oracle_start(ob, w):
+    """The benchmark's start state scored by the oracle (FP64)."""
     rng = np.random.default_rng(12)
     th, phi = synth.start_states(w, w.nchain, rng)
     S = w.batch.n_subject
     lp = np.stack([ob.logprior(w.p_prior, th[s]) for s in range(S)])
     ll = ob.loglik(w.model, w.batch, th)
+    pst = None
     if phi is not None:
-        plp = ob.logprior(w.h_prior, phi)
-        pll = ob.loghlike(w.p_prior, phi, th)
+        pst = (phi, ob.logprior(w.h_prior, phi), ob.loghlike(w.p_prior, phi, th))
+    return pst, (th, lp, ll)
+
+
+def cpu_baseline(w, n_sweeps=1, threads=None):
+    """The oracle's -O3 build on the host cores: one replica of n_sweeps
+    sweeps of the full workload alone (the single-thread rate, as one
+    reference instance runs), then `threads` replicas at once (all cores, as
+    the reference's independent instances run); FP64, reference chain order."""
+    from oracle import binding as ob
+    ob.build()
+    phi, subj = oracle_start(ob, w)
     cfg = cfg_for(w, n_sweeps, abi.FP64)
     threads = threads or os.cpu_count() or 1
     times = [0.0] * threads
@@ -233,24 +231,66 @@ def cpu_baseline(w, n_sweeps=1, threads=None):
         c = abi.DEConfigPy(**{**cfg.__dict__, "seed": 1000 + k})
         t0 = time.perf_counter()
         if phi is not None:
-            ob.run(c, w.model, w.batch, w.p_prior, w.h_prior, (phi, plp, pll), (th, lp, ll))
+            ob.run(c, w.model, w.batch, w.p_prior, w.h_prior, phi, subj)
         else:
-            ob.run_subjects(c, w.model, w.batch, w.p_prior, th, lp, ll)
+            ob.run_subjects(c, w.model, w.batch, w.p_prior, *subj)
         times[k] = time.perf_counter() - t0
 
-    ts = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
-    t0 = time.perf_counter()
-    for t in ts:
-        t.start()
-    for t in ts:
-        t.join()
-    wall = time.perf_counter() - t0
+    ob.use_build(fast=True)
+    try:
+        one(0)
+        single = times[0]
+        ts = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
+        t0 = time.perf_counter()
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        wall = time.perf_counter() - t0
+    finally:
+        ob.use_build(fast=False)
     sweeps = threads * n_sweeps
     return {"value": sweeps / wall, "unit": "DE sweeps/s", "cores": threads, "kind": "port",
-            "sample": f"{threads} replicas x {n_sweeps} sweep(s) of the full {w.name} "
-                      f"workload, oracle/ FP64 C restatement, one thread each",
-            "wall_s": wall, "single_replica_s": float(np.median(times)),
+            "sample": f"{threads} concurrent replicas x {n_sweeps} sweep(s) of the full {w.name} "
+                      f"workload (after one replica alone), oracle/ FP64 C restatement built -O3, "
+                      f"one thread each",
+            "single_thread_sweeps_per_s": n_sweeps / single,
+            "wall_s": wall, "single_replica_s": single,
             "trial_logl_evals_per_s": sweeps * w.nchain * len(w.batch.rt) / wall}
+
+
+def oracle_accuracy(w, h, theta):
+    """Errors against the oracle (FP64) at the chain states theta [S][C][P]:
+    every per-subject sum of the MIXED likelihood through ggdmc_loglik, and
+    per trial through ggdmc_trial_logdens for each subject's first chain."""
+    from oracle import binding as ob
+    ob.build()
+    mixed = h.loglik(theta, abi.MIXED)
+    want = ob.loglik(w.model, w.batch, theta)
+    t32 = h.trial_logdens(theta[:, 0], abi.MIXED)
+    t64 = np.concatenate([ob.sumloglike(w.model, w.batch.subject(s).rt, w.batch.subject(s).cell,
+                                        theta[s, 0], per_trial=True)[1] for s in range(w.batch.n_subject)])
+    return {"max_rel_err_per_sum": float(np.max(np.abs(mixed - want) / np.abs(want))),
+            "max_abs_err_per_sum": float(np.max(np.abs(mixed - want))),
+            "max_abs_err_per_trial": float(np.max(np.abs(t32 - t64))),
+            "median_abs_err_per_trial": float(np.median(np.abs(t32 - t64))),
+            "mean_err_per_trial": float(np.mean(t32 - t64)),
+            "sums": int(want.size), "trials": int(t64.size),
+            "state": "the chains after the timed sweeps"}
+
+
+def config_of(w, world=1):
+    """The workload's description, the same in both arms' lines."""
+    S, Cn, P = w.batch.n_subject, w.nchain, w.model.n_par
+    c = {"workload": w.name, "subjects": S, "trials": int(len(w.batch.rt)),
+         "accumulators": int(w.model.n_acc), "npar": P, "nphi": 2 * P if w.hierarchical else 0,
+         "chains": Cn, "pop_migration_prob": 0.05 if w.hierarchical else 0.0, "sub_migration_prob": 0.06,
+         "chain_order": "reference (in place, in order)",
+         "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+         "l2": "flushed between sweeps (256 MB memset, excluded from the timing)"}
+    if w.name == WORKLOAD:
+        c["trials_per_subject"] = "U{100..2000}"
+    return c
 
 
 def run_ours(args):
@@ -310,8 +350,10 @@ def run_ours(args):
                 "fp64_batched_sweeps_per_s": round(fp64_sweeps_s, 3),
                 "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
                 "clocks": clk.summary()}
+        line["config"] = config_of(w, world)
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(w, 1)
+            line["accuracy_vs_oracle"] = oracle_accuracy(w, h, out["theta"])
         print(json.dumps(line), flush=True)
         return
 
@@ -328,6 +370,7 @@ def run_ours(args):
     # end to end through the one-shot C ABI with host buffers: upload of the
     # trials and chain states, the sweeps, download of every sample
     e2e_steps = min(args.steps, E2E_MAX_STEPS)
+    gpu.run(cfg_for(w, e2e_steps, abi.MIXED), w.model, w.batch, w.p_prior, w.h_prior, phi, subj)  # warm-up
     t0 = time.perf_counter()
     e2e = gpu.run(cfg_for(w, e2e_steps, abi.MIXED), w.model, w.batch, w.p_prior, w.h_prior,
                   phi, subj)
@@ -350,12 +393,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic (seeded LBA race simulation of the named shapes)",
-        "config": {"workload": WORKLOAD, "subjects": S, "trials": int(len(w.batch.rt)),
-                   "trials_per_subject": "U{100..2000}", "accumulators": K_ACC,
-                   "npar": P, "nphi": 2 * P, "chains": Cn, "pop_migration_prob": 0.05,
-                   "sub_migration_prob": 0.06, "chain_order": "reference (in place, in order)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "flushed between sweeps (256 MB memset, excluded from the timing)"},
+        "config": config_of(w, world),
         "trial_logl_evals_per_s": round(evals_s * world, 1),
         "fp64_fallback_fraction": round(st["fallbacks"] / max(st["trial_evals"], 1), 6),
         "fp64_plain_sweeps_per_s": round(plain_sweeps_s, 3),
@@ -383,12 +421,14 @@ def run_ours(args):
         "e2e": {"value": round(e2e_steps / e2e_s, 3), "unit": "DE sweeps/s",
                 "h2d_bytes_per_step": int(h2d // e2e_steps), "d2h_bytes_per_step": int(d2h // e2e_steps),
                 "steps": e2e_steps,
-                "call": "ggdmc_run (one-shot C ABI: upload, sweeps, sample download)"},
+                "call": "ggdmc_run (one-shot C ABI: upload, sweeps, sample download; "
+                        "one untimed call first)"},
         "clocks": clk.summary(),
         "wall_s_timed_run": round(wall, 3),
     }
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(w, 1)
+        line["accuracy_vs_oracle"] = oracle_accuracy(w, h, out["theta"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -403,8 +443,6 @@ def run_reference(args):
     from oracle import binding as ob
     ob.build()
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
     # each step: one sweep per replica, all host threads
     vals = []
     t_all = time.perf_counter()
@@ -418,8 +456,7 @@ def run_reference(args):
         "n_gpus": world, "steps": len(vals), "warmup": 0,
         "ms_per_step": round(1e3 / v, 2), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "subjects": w.batch.n_subject,
-                   "trials": int(len(w.batch.rt)), "chains": w.nchain},
+        "config": config_of(w, world),
         "trial_logl_evals_per_s": round(float(np.median([x["trial_logl_evals_per_s"] for x in vals])), 1),
         "cpu_baseline": {**vals[0], "value": round(v, 4)},
         "e2e": {"value": round(v, 4), "unit": "DE sweeps/s", "h2d_bytes_per_step": 0,

@@ -75,6 +75,10 @@ class Workload:
     pop_scale: np.ndarray | None
     nchain: int
     hierarchical: bool
+    # a stored start state (theta [S][C][P], phi [C][2P] or None), used
+    # instead of chains scattered around theta_true
+    start_theta: np.ndarray | None = None
+    start_phi: np.ndarray | None = None
 
 
 def unif_prior(P, lo=0.0, hi=10.0):
@@ -217,7 +221,11 @@ def hier_ddm_64(seed: int = 3, n_subject: int = 64, n: int = 500, dt: float = 1e
 
 def start_states(w: Workload, nchain: int, rng, spread: float = 0.05):
     """Chains scattered around the generating values (theta [S][C][P] and,
-    for hierarchical workloads, phi [C][2P]); lp / ll left for the caller."""
+    for hierarchical workloads, phi [C][2P]), or the workload's stored start
+    state; lp / ll left for the caller."""
+    if w.start_theta is not None:
+        phi = w.start_phi[:nchain] if w.start_phi is not None else None
+        return np.array(w.start_theta[:, :nchain]), (np.array(phi) if phi is not None else None)
     S, P = w.theta_true.shape
     th = w.theta_true[:, None, :] * (1.0 + spread * rng.standard_normal((S, nchain, P)))
     th = np.abs(th)
@@ -227,3 +235,23 @@ def start_states(w: Workload, nchain: int, rng, spread: float = 0.05):
         sca = w.pop_scale[None, :] * (1.0 + spread * rng.standard_normal((nchain, P)))
         phi = np.concatenate([np.abs(loc), np.abs(sca)], axis=1)
     return th, phi
+
+
+def fixture_lba_768(npz: str, hierarchical: bool, nchain: int = 39) -> Workload:
+    """The reference fixture lba_data6.rda's own data (tests/golden/lba_fx6.npz):
+    the 13-parameter, 2-accumulator design with 768 trials per subject, and
+    its stored start samples.  Single subject: its sub_dmi, U(0, 10) priors
+    and sub_samples; hierarchical: the 32 pop_dmis, pop_priors and the phi and
+    subject chains of pop_samples (the first nchain of them)."""
+    z = np.load(npz)
+    model = FlatModel(0, list(z["pnames"]), list(z["accumulators"]), list(z["cell_names"]),
+                      z["constants"], list(z["const_names"]), z["param_src"], z["resp"])
+    if not hierarchical:
+        batch = SubjectBatch(z["sub_rt"], z["sub_cell"], np.array([0, len(z["sub_rt"])], np.int64))
+        th = z["sub_theta"][None, :nchain]
+        return Workload("single_lba_768", model, batch, th[:, 0], z["sub_prior"], None, None, None,
+                        nchain, False, start_theta=th)
+    batch = SubjectBatch(z["pop_rt"], z["pop_cell"], z["pop_offsets"])
+    th = z["subj_theta"][:, :nchain]
+    return Workload("hier_lba_32", model, batch, th[:, 0], z["pop_p_prior"], z["pop_h_prior"], None, None,
+                    nchain, True, start_theta=th, start_phi=z["phi_theta"][:nchain])

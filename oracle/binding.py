@@ -16,24 +16,34 @@ import numpy as np
 from ggdmc_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libggdmc_oracle.so")
+LIB_PATH = os.path.join(HERE, "libggdmc_oracle.so")            # parity build
+FAST_PATH = os.path.join(HERE, "libggdmc_oracle_fast.so")      # timed CPU baseline
 
-_lib = None
+_libs = {}
+_use_fast = False
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc, a second or two)."""
-    if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "ggdmc_oracle.c")):
+    """Compile both oracle builds with the Makefile (gcc, a few seconds)."""
+    src = os.path.getmtime(os.path.join(HERE, "ggdmc_oracle.c"))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src for p in (LIB_PATH, FAST_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
+def use_build(fast: bool) -> None:
+    """Route the functions below to the -O3 build (the timed CPU baseline)
+    or back to the parity build (the default; every parity check uses it)."""
+    global _use_fast
+    _use_fast = bool(fast)
+
+
 def lib():
-    global _lib
-    if _lib is None:
+    path = FAST_PATH if _use_fast else LIB_PATH
+    L = _libs.get(path)
+    if L is None:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         P = C.POINTER
         L.oracle_uniform.restype = C.c_double
         L.oracle_uniform.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int64, C.c_int64]
@@ -65,8 +75,8 @@ def lib():
                                  P(abi.Prior), P(abi.ChainState), P(abi.ChainState),
                                  P(C.c_double), P(abi.Samples), P(abi.Samples),
                                  P(abi.RunStats)]
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return L
 
 
 def uniform(seed, it, level, pass_, slot) -> float:

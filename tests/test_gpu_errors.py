@@ -39,17 +39,23 @@ def test_deadline_returns_timeout_and_handle_recovers(oracle, monkeypatch):
 
 
 def test_device_wait_gives_up_and_handle_recovers(oracle, monkeypatch):
-    """The fused schedule's idle CTAs poll for work with a limit; with the
-    limit at 0 polls they give up at once, the kernel sets the run's status
-    and returns (no GPU wait is left running), the host reports
-    GGDMC_ERR_TIMEOUT, and the same handle then reproduces the oracle."""
+    """The fused schedule's idle CTAs poll for work with a limit.  One fit of
+    6000 trials among 300 fits of 20-40: the other CTAs finish their fits and
+    wait while it is resolved; with the limit at 0 polls they give up at once,
+    the kernel sets the run's status and returns (no GPU wait is left
+    running), the host reports GGDMC_ERR_TIMEOUT, and the same handle then
+    reproduces the oracle."""
+    from ggdmc_gb300.dmi import SubjectBatch
     monkeypatch.setenv("GGDMC_FUSED", "1")
-    w = synth.many_fits_1024(n_fit=400, n_lo=100, n_hi=900)      # several waves of fits per SM
+    w = synth.many_fits_1024(n_fit=300, n_lo=20, n_hi=40)
+    long_fit = synth.simulate_subject(w.model, w.theta_true[0], 6000, np.random.default_rng(1), "long")
+    subs = [long_fit] + [w.batch.subject(f) for f in range(1, 300)]
+    batch = SubjectBatch.pack(subs)
     C = 27
     th, _ = synth.start_states(w, C, np.random.default_rng(6))
-    lp = np.stack([oracle.logprior(w.p_prior, th[f]) for f in range(w.batch.n_subject)])
-    ll = oracle.loglik(w.model, w.batch, th)
-    h = gpu.Handle(w.model, w.batch)
+    lp = np.stack([oracle.logprior(w.p_prior, th[f]) for f in range(batch.n_subject)])
+    ll = oracle.loglik(w.model, batch, th)
+    h = gpu.Handle(w.model, batch)
     cfg = abi.DEConfigPy(nchain=C, nparameter=w.model.n_par, nmc=6, thin=1, sub_migration_prob=0.06,
                          seed=9, precision=abi.FP64)
     monkeypatch.setenv("GGDMC_SPEC_IDLE_LIMIT", "0")
@@ -58,6 +64,6 @@ def test_device_wait_gives_up_and_handle_recovers(oracle, monkeypatch):
     assert e.value.status == abi.GGDMC_ERR_TIMEOUT
     monkeypatch.delenv("GGDMC_SPEC_IDLE_LIMIT")
     out = h.run(cfg, w.p_prior, th, lp, ll)
-    want = oracle.run_subjects(cfg, w.model, w.batch, w.p_prior, th, lp, ll)
+    want = oracle.run_subjects(cfg, w.model, batch, w.p_prior, th, lp, ll)
     assert np.array_equal(out["theta"], want["theta"])
     assert np.array_equal(out["s_theta"], want["s_theta"])

@@ -121,7 +121,7 @@ def test_run_hyper_host_fed_draws(oracle):
     lp = oracle.logprior(z["pop_h_prior"], theta)
     ll = oracle.loghlike(z["pop_p_prior"], theta, np.repeat(rows[:, None, :], C, axis=1))
     for blocked in (False, True):
-        cfg = abi.DEConfigPy(nchain=C, nparameter=2 * model.n_par, nmc=5, thin=1,
+        cfg = abi.DEConfigPy(nchain=C, nparameter=2 * model.n_par, nmc=10, thin=1,
                              sub_migration_prob=0.25, is_pblocked=blocked, seed=0)
         ni, npass, ns = abi.draw_layout(cfg, 1, False)
         draws = np.random.default_rng(23).random(ni * npass * ns)
