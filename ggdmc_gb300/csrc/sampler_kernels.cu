@@ -23,6 +23,7 @@
 #include <climits>
 #include <cstdint>
 
+#include "dfloat.h"
 #include "sampler.cuh"
 
 // k_sub_resolve's block: 512 threads, one CTA per SM (128 registers a thread;
@@ -365,15 +366,11 @@ __device__ void build_tables64(const RunDev &r, SubSmem &sm, const double *theta
         sm.t064[q] = src_value(r.m.t0_src[q], theta, r.m.consts);
 }
 
-// FP32 trial constants of tuple u of theta (Ent32, device_common.cuh), each
-// formed in FP64 and split into hi + lo FP32 parts, and lg = log g.  Returns
-// false when the tuple is outside the FP32 form's domain.
-__device__ __forceinline__ void split_f(double x, float &h, float &l)
-{
-    h = (float)x;
-    l = (float)(x - (double)h);
-}
-
+// FP32 trial constants of tuple u of theta (Ent32, device_common.cuh) and
+// lg = log g, in double-float FP32 arithmetic (dfloat.h; about 1e-10
+// relative, where FP64 erfc, log and divisions here cost the proposal kernel
+// more than the rest of its work).  Returns false when the tuple is outside
+// the FP32 form's domain (Phi(v/s) below 1e-30, or a constant not finite).
 __device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, int u, Ent32 &E, double &lg)
 {
     const EntSrc es = r.m.ent_src[u];
@@ -381,21 +378,20 @@ __device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, in
     const double B = src_value(es.B, theta, r.m.consts);
     const double v = src_value(es.v, theta, r.m.consts);
     const double s = src_value(es.s, theta, r.m.consts);
-    const double is = 1.0 / s;
-    const double kap = v * is;
-    // Phi(kappa) and Phi(-kappa) from one erfc, each with full relative accuracy
-    const double tl = 0.5 * erfc(fabs(kap) * 0.70710678118654752440);
-    const double den = (kap >= 0.0) ? 1.0 - tl : tl, qt = (kap >= 0.0) ? tl : 1.0 - tl;
-    const double g = s / (A * den), q = qt / den;
-    split_f((A + B) * is, E.a.x, E.b.x);
-    split_f(B * is, E.a.y, E.b.y);
-    split_f(kap, E.a.z, E.b.z);
-    split_f(0.5 * A * is, E.a.w, E.b.w);
-    split_f(g, E.c.x, E.c.y);
-    split_f(q, E.c.z, E.c.w);
-    lg = log(g);
-    return A > 0.0 && s > 0.0 && den > 1e-30 && isfinite(E.a.x) && isfinite(E.a.y) && isfinite(E.a.z) &&
-           isfinite(E.c.x) && isfinite(E.c.z) && E.a.w > 0.f && E.c.x > 0.f && isfinite(lg);
+    const dfl Ad = df_from_double(A), Bd = df_from_double(B), sd = df_from_double(s);
+    const dfl is = df_div(dfl{1.f, 0.f}, sd);
+    const dfl kap = df_mul(df_from_double(v), is);
+    dfl den, qt;                                    // Phi(kappa), Phi(-kappa)
+    df_phi_pair(kap, den, qt);
+    const dfl g = df_div(sd, df_mul(Ad, den)), q = df_div(qt, den);
+    const dfl ab = df_mul(df_add(Ad, Bd), is), bs = df_mul(Bd, is), ha = df_mul_f(df_mul(Ad, is), 0.5f);
+    E.a = make_float4(ab.h, bs.h, kap.h, ha.h);
+    E.b = make_float4(ab.l, bs.l, kap.l, ha.l);
+    E.c = make_float4(g.h, g.l, q.h, q.l);
+    const bool ok = A > 0.0 && s > 0.0 && den.h > 1e-30f && isfinite(ab.h) && isfinite(bs.h) && isfinite(kap.h) &&
+                    isfinite(g.h) && isfinite(q.h) && ha.h > 0.f && g.h > 0.f;
+    lg = ok ? df_to_double(df_log(g)) : 0.0;
+    return ok;
 }
 
 __device__ __forceinline__ float2 t0split(const RunDev &r, const double *theta, int q)
@@ -593,7 +589,9 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
                                                  float (&kc)[kGroup], int (&es)[kGroup], int (&nfb)[kGroup])
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0, KR = r.m.n_acc;
-#pragma unroll
+    // not unrolled: one copy of the density loop, and the per-proposal sums
+    // (stored once per proposal) need no registers across it
+#pragma unroll 1
     for (int g = 0; g < kGroup; ++g) {
         if (!ok[g]) continue;                       // uniform over the block
         const Ent32 *E = sm.e32 + g * NE;
