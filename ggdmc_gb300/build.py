@@ -18,8 +18,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libggdmc_gpu.so")
 SOURCES = ["sampler_kernels.cu", "runtime.cu", "peak.cu"]
-C_SOURCES = ["dmi_convert.c"]            # host-only C, compiled by gcc
-HEADERS = ["device_common.cuh", "model_tables.h", "sampler.cuh"]
+C_SOURCES = ["dmi_convert.c", "posterior_merge.c"]   # host-only C, compiled by gcc
+HEADERS = ["device_common.cuh", "dfloat.h", "model_tables.h", "sampler.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -37,8 +37,7 @@ def _stale() -> bool:
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
     deps += [os.path.join(CSRC, f) for f in C_SOURCES]
-    deps.append(os.path.join(ROOT, "include", "ggdmc_gpu.h"))
-    deps.append(os.path.join(ROOT, "include", "ggdmc_dmi.h"))
+    deps += [os.path.join(ROOT, "include", f) for f in ("ggdmc_gpu.h", "ggdmc_dmi.h", "ggdmc_post.h")]
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 

@@ -79,6 +79,9 @@ def lib():
     L.ggdmc_handle_run.argtypes = [C.c_void_p, P(abi.DEConfig), P(abi.Prior), P(abi.Prior),
                                    P(abi.ChainState), P(abi.ChainState), P(C.c_double),
                                    P(abi.Samples), P(abi.Samples), P(abi.RunStats)]
+    L.ggdmc_rebuild_posterior.restype = St
+    L.ggdmc_rebuild_posterior.argtypes = [P(abi.Samples), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                          P(abi.Samples)]
     L.ggdmc_probe_peaks.restype = St
     L.ggdmc_probe_peaks.argtypes = [P(C.c_double), P(C.c_double)]
     _lib = L
@@ -282,3 +285,32 @@ def loghlike(p_table, phi, subj_theta):
     check(lib().ggdmc_loghlike(C.byref(p), abi.dptr(ph), abi.dptr(st), st.shape[0], ph.shape[0],
                                abi.dptr(out)))
     return out
+
+
+def rebuild_posterior(fits):
+    """RebuildPosterior / RebuildHyper (R/parallel_helper.R:62-109) through
+    ggdmc_rebuild_posterior: fits is a list of (theta [nmc][C][P], lp [nmc][C],
+    ll [nmc][C]) sample sets of one level (for example the levels of a
+    run_subjects call on one subject's data replicated, or the phi samples of
+    several hierarchical runs).  Returns (theta [nmc*C][F][P], lp, ll [nmc*C][F])
+    in the reference's merged order.  Host code only: needs no GPU."""
+    fits = [tuple(np.ascontiguousarray(a, np.float64) for a in f) for f in fits]
+    nmc, nchain, npar = fits[0][0].shape
+    for th, lp, ll in fits:
+        if th.shape != (nmc, nchain, npar) or lp.shape != (nmc, nchain) or ll.shape != (nmc, nchain):
+            raise ValueError("every fit needs theta [nmc][nchain][npar] and lp, ll [nmc][nchain] of one shape")
+    F = len(fits)
+    arr = (abi.Samples * F)(*[abi.Samples(abi.dptr(th), abi.dptr(lp), abi.dptr(ll)) for th, lp, ll in fits])
+    th = np.zeros((nmc * nchain, F, npar))
+    lp = np.zeros((nmc * nchain, F))
+    ll = np.zeros((nmc * nchain, F))
+    out = abi.Samples(abi.dptr(th), abi.dptr(lp), abi.dptr(ll))
+    check(lib().ggdmc_rebuild_posterior(arr, F, nmc, nchain, npar, C.byref(out)))
+    return th, lp, ll
+
+
+def rebuild_posteriors(runs):
+    """RebuildPosteriors (R/parallel_helper.R:162-208): the subject samples of
+    several hierarchical runs (each a gpu.run result) merged per subject."""
+    S = runs[0]["subj_s"][0].shape[0]
+    return [rebuild_posterior([tuple(x[s] for x in r["subj_s"]) for r in runs]) for s in range(S)]
