@@ -58,6 +58,14 @@ class Samples(C.Structure):
     _fields_ = [("theta", _dp), ("lp", _dp), ("ll", _dp)]
 
 
+class Diag(C.Structure):
+    _fields_ = [("mean", _dp), ("sd", _dp), ("naive_se", _dp), ("ts_se", _dp), ("quantiles", _dp),
+                ("psrf", _dp)]
+
+
+PSRF_REFERENCE, PSRF_CODA = 0, 1
+
+
 class RunStats(C.Structure):
     _fields_ = [("proposals", C.c_int64), ("accepts", C.c_int64), ("migrations", C.c_int64),
                 ("reevaluations", C.c_int64), ("kernel_launches", C.c_int64),

@@ -17,9 +17,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libggdmc_gpu.so")
-SOURCES = ["sampler_kernels.cu", "runtime.cu", "peak.cu"]
+SOURCES = ["sampler_kernels.cu", "runtime.cu", "diag_kernels.cu", "peak.cu"]
 C_SOURCES = ["dmi_convert.c", "posterior_merge.c"]   # host-only C, compiled by gcc
-HEADERS = ["device_common.cuh", "dfloat.h", "model_tables.h", "sampler.cuh"]
+HEADERS = ["device_common.cuh", "dfloat.h", "fquantile.h", "model_tables.h", "sampler.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -1396,6 +1396,70 @@ ggdmc_status ggdmc_handle_summary(ggdmc_handle *h, int32_t start, double *mean, 
     return s;
 }
 
+ggdmc_status ggdmc_handle_diagnostics(ggdmc_handle *h, int32_t start, int32_t end, const double *probs,
+                                      int32_t n_prob, double conf, int32_t psrf_form, ggdmc_diag *subj,
+                                      ggdmc_diag *phi)
+{
+    if (!h) return fail(GGDMC_ERR_ARG, "handle is NULL");
+    if (h->last_nmc < 1) return fail(GGDMC_ERR_ARG, "no run has stored samples on this handle");
+    const int nmc = h->last_nmc, C = h->last_C;
+    if (end <= 0) end = nmc;
+    if (start < 0 || end > nmc || end - start < 2)
+        return fail(GGDMC_ERR_ARG, "diagnostics need 0 <= start, end <= nmc and two or more iterations");
+    const int n = end - start;
+    if (diag_kmax(n) > kDiagMaxLag) return fail(GGDMC_ERR_ARG, "diagnostics take at most 2.5e6 iterations");
+    if (n_prob == 1) return fail(GGDMC_ERR_ARG, "prob must be more than one element");
+    if (n_prob < 0 || n_prob > kDiagMaxProb || (n_prob > 0 && !probs))
+        return fail(GGDMC_ERR_ARG, "n_prob must be 0 or 2..16 with probs given");
+    for (int i = 0; i < n_prob; ++i)
+        if (!(probs[i] >= 0.0 && probs[i] <= 1.0)) return fail(GGDMC_ERR_ARG, "probs must lie in [0, 1]");
+    if (psrf_form != GGDMC_PSRF_REFERENCE && psrf_form != GGDMC_PSRF_CODA)
+        return fail(GGDMC_ERR_ARG, "psrf_form must be GGDMC_PSRF_REFERENCE or GGDMC_PSRF_CODA");
+    cudaStream_t st = h->stream;
+    DevBuf<double> dprobs;
+    if (n_prob > 0) {
+        CU(dprobs.alloc(n_prob));
+        CU(cudaMemcpyAsync(dprobs.p, probs, sizeof(double) * n_prob, cudaMemcpyHostToDevice, st));
+    }
+    auto level = [&](const double *smp, int L, int P, ggdmc_diag *o) -> ggdmc_status {
+        if (!o || L < 1 || P < 1) return GGDMC_OK;
+        if (o->psrf && C < 3) return fail(GGDMC_ERR_ARG, "Minimum three chains needed");
+        if (o->psrf && !(conf > 0.0 && conf < 1.0)) return fail(GGDMC_ERR_ARG, "conf must lie in (0, 1)");
+        const bool wform = o->psrf && psrf_form == GGDMC_PSRF_REFERENCE;
+        if (wform && P > kDiagMaxPsrfPar)
+            return fail(GGDMC_ERR_ARG, "the reference PSRF form takes at most 64 parameters a level");
+        const size_t LP = (size_t)L * P;
+        DevBuf<double> cstat, wcov, out;
+        CU(cstat.alloc(LP * C * 3));
+        if (wform) CU(wcov.alloc(LP * C * P));
+        // outputs side by side: mean, sd, naive, ts [LP] each, quantiles [LP][n_prob], psrf [LP][2]
+        const size_t oq = 4 * LP, opsrf = oq + LP * n_prob, ntot = opsrf + 2 * LP;
+        CU(out.alloc(ntot));
+        double *q = out.p;
+        CU(launch_diagnostics(smp, L, nmc, C, P, start, n, dprobs.p, o->quantiles ? n_prob : 0, conf, psrf_form,
+                              cstat.p, wcov.p, q, q + LP, q + 2 * LP, q + 3 * LP,
+                              (o->quantiles && n_prob > 0) ? q + oq : nullptr, o->psrf ? q + opsrf : nullptr, st));
+        std::vector<double> host(ntot);
+        CU(cudaMemcpyAsync(host.data(), out.p, sizeof(double) * ntot, cudaMemcpyDeviceToHost, st));
+        ggdmc_status ws = wait_stream(st);
+        if (ws) return ws;
+        auto put = [&](double *dst, size_t off, size_t cnt) {
+            if (dst) std::memcpy(dst, host.data() + off, sizeof(double) * cnt);
+        };
+        put(o->mean, 0, LP);
+        put(o->sd, LP, LP);
+        put(o->naive_se, 2 * LP, LP);
+        put(o->ts_se, 3 * LP, LP);
+        if (n_prob > 0) put(o->quantiles, oq, LP * n_prob);
+        put(o->psrf, opsrf, 2 * LP);
+        return GGDMC_OK;
+    };
+    ggdmc_status s = level(h->smp_th.p, h->last_S, h->last_P, subj);
+    if (s) return s;
+    if (h->last_Pphi > 0) s = level(h->psmp_th.p, 1, h->last_Pphi, phi);
+    return s;
+}
+
 ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta, int32_t precision, double *out)
 {
     if (!h || !theta || !out) return fail(GGDMC_ERR_ARG, "bad trial_logdens arguments");

@@ -139,6 +139,18 @@ cudaError_t launch_init_draw(const double *rows, int P, int C, int level0, int n
                              const uint8_t *done, uint64_t seed, double *theta, cudaStream_t st);
 cudaError_t launch_summary(const double *smp, int L, int nmc, int C, int P, int start, double *cs,
                            double *mean, double *sd, double *psrf, cudaStream_t st);
+// Posterior diagnostics (diag_kernels.cu) of samples smp [L][nmc][C][P],
+// iterations [start, start + n): cstat [L][C*P][3] and (form 0 with psrf)
+// wcov [L][C][P][P] are scratch; mean, sd, nse, tse [L][P], quant
+// [L][P][n_prob] (probs on the device), psrf [L][P][2]; any output may be
+// NULL.  form 0: the reference's PSRF, 1: coda's.
+constexpr int kDiagMaxLag = 64;       // kmax = min(n - 1, floor(10 log10 n)) <= 64: n < 2.5e6
+constexpr int kDiagMaxPsrfPar = 64;   // P of the reference's PSRF form (the P x P covariances)
+constexpr int kDiagMaxProb = 16;
+int diag_kmax(int n);
+cudaError_t launch_diagnostics(const double *smp, int L, int nmc, int C, int P, int start, int n, const double *probs,
+                               int n_prob, double conf, int form, double *cstat, double *wcov, double *mean,
+                               double *sd, double *nse, double *tse, double *quant, double *psrf, cudaStream_t st);
 cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
                             cudaStream_t st);
 cudaError_t launch_loghlike(const RunDev &r, const double *phi, double *out, cudaStream_t st);

@@ -1,5 +1,6 @@
 """Posterior diagnostics of sampled chains: summaries and the Brooks-Gelman
-potential scale reduction factor.
+potential scale reduction factor (host restatements; the device computes the
+same quantities in ggdmc_handle_diagnostics).
 
 The samples are in the C ABI's layout [nmc][nchain][npar], which is R's
 posterior@theta [npar, nchain, nmc].
@@ -77,14 +78,78 @@ def gelman(samples, start: int = 0, end: int | None = None, conf: float = 0.95,
     return {"psrf": psrf, "mpsrf": mpsrf}
 
 
-def summary(samples, start: int = 0, end: int | None = None,
-            probs=(0.025, 0.25, 0.5, 0.75, 0.975)) -> dict:
-    """Mean, sd and quantiles per parameter over all chains and iterations,
-    and the standard error of the mean from the chain means (chains as
-    independent replicates)."""
+def spectrum0_ar(x) -> tuple[float, int]:
+    """The spectral density at frequency zero of one chain from an AR fit,
+    as R/model-class.R:257-275 (spectrum0_ar, which safespec0 wraps) computes
+    it: 0 when the residual sd of lm(x ~ 1:n) is within all.equal's 1.5e-8 of
+    zero; otherwise the Yule-Walker AR fit of stats::ar (order chosen by AIC
+    up to min(n - 1, floor(10 log10 n)), autocovariances of the demeaned
+    chain with denominator n, innovations variance scaled by n / (n - order -
+    1)) and var.pred / (1 - sum(ar))^2.  Returns (spectrum, order)."""
+    x = np.asarray(x, np.float64)
+    n = x.size
+    if n < 2:
+        return float("nan"), 0
+    xc = x - x.mean()
+    zc = np.arange(n) - (n - 1) / 2.0
+    sxz, szz = float(zc @ xc), float(zc @ zc)
+    rss = max(float(xc @ xc) - sxz * sxz / szz, 0.0)
+    if np.sqrt(rss / (n - 1)) <= 1.5e-8:
+        return 0.0, 0
+    kmax = min(n - 1, int(np.floor(10 * np.log10(n))))
+    r = np.array([xc[: n - k] @ xc[k:] for k in range(kmax + 1)]) / n
+    # Durbin-Levinson recursion for the Yule-Walker equations of orders 1..kmax
+    var = np.empty(kmax + 1)
+    var[0] = r[0]
+    coef = [np.zeros(0)]
+    phi = np.zeros(0)
+    for k in range(1, kmax + 1):
+        a = (r[k] - phi @ r[k - 1:0:-1]) / var[k - 1]
+        phi = np.concatenate([phi - a * phi[::-1], [a]])
+        var[k] = var[k - 1] * (1.0 - a * a)
+        coef.append(phi)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        aic = n * np.log(var) + 2.0 * np.arange(kmax + 1)
+    order = int(np.nanargmin(aic))
+    vp = var[order] * n / (n - (order + 1))
+    return float(vp / (1.0 - coef[order].sum()) ** 2), order
+
+
+def quantile7(x, probs) -> np.ndarray:
+    """Quantiles of type 7 as R's quantile / matrixStats::rowQuantiles form
+    them: h = 1 + (n - 1) p, (1 - (h - lo)) x[lo] + (h - lo) x[hi] of the
+    sorted values (1-based lo = floor h, hi = ceiling h); x[lo] when the two
+    order statistics are equal."""
+    xs = np.sort(np.asarray(x, np.float64))
+    n = xs.size
+    out = np.empty(len(probs))
+    for i, p in enumerate(probs):
+        h = (n - 1) * p
+        lo = int(np.floor(h))
+        hi = min(lo + 1, n - 1)
+        g = h - lo
+        out[i] = xs[lo] if (g == 0.0 or xs[hi] == xs[lo]) else (1.0 - g) * xs[lo] + g * xs[hi]
+    return out
+
+
+def summary(samples, start: int = 0, end: int | None = None, probs=(0.05, 0.5, 0.975)) -> dict:
+    """summary of a posterior (R/model-class.R:370-424) over iterations
+    [start, end) of samples [nmc][nchain][npar] (R's start is 1-based and its
+    end inclusive): per parameter over all chains and iterations the Mean,
+    the SD, the Naive SE sqrt(var / niter * nchain) and the Time-series SE
+    sqrt(mean_k spectrum0(chain k) / niter * nchain) -- the reference's
+    formulas as written -- and the quantiles of type 7 at probs (the
+    reference's default 0.05, 0.5, 0.975).  se_mean is the standard error of
+    the mean from the chain means (chains as independent replicates)."""
     th = _theta(samples)[start:end]
-    flat = th.reshape(-1, th.shape[2])
+    niter, nchain, npar = th.shape
+    flat = th.reshape(-1, npar)
+    var = flat.var(axis=0, ddof=1)
+    ts = np.array([[spectrum0_ar(th[:, k, p])[0] for p in range(npar)] for k in range(nchain)])
     cm = th.mean(axis=0)
-    return {"mean": flat.mean(axis=0), "sd": flat.std(axis=0, ddof=1),
-            "quantiles": np.quantile(flat, probs, axis=0), "probs": np.asarray(probs),
-            "se_mean": cm.std(axis=0, ddof=1) / np.sqrt(th.shape[1])}
+    return {"mean": flat.mean(axis=0), "sd": np.sqrt(var),
+            "naive_se": np.sqrt(var / niter * nchain),
+            "ts_se": np.sqrt(ts.mean(axis=0) / niter * nchain),
+            "quantiles": np.stack([quantile7(flat[:, p], probs) for p in range(npar)], axis=1),
+            "probs": np.asarray(probs),
+            "se_mean": cm.std(axis=0, ddof=1) / np.sqrt(nchain)}

@@ -58,6 +58,9 @@ def lib():
                                    C.c_uint64, C.c_int32, P(abi.ChainState), P(abi.ChainState)]
     L.ggdmc_handle_summary.restype = St
     L.ggdmc_handle_summary.argtypes = [C.c_void_p, C.c_int32] + [P(C.c_double)] * 6
+    L.ggdmc_handle_diagnostics.restype = St
+    L.ggdmc_handle_diagnostics.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(C.c_double), C.c_int32,
+                                           C.c_double, C.c_int32, P(abi.Diag), P(abi.Diag)]
     L.ggdmc_loghlike.restype = St
     L.ggdmc_loghlike.argtypes = [P(abi.Prior), P(C.c_double), P(C.c_double), C.c_int32,
                                  C.c_int32, P(C.c_double)]
@@ -181,6 +184,30 @@ class Handle:
         if phi:
             out["phi"] = (pm, ps, pr)
         return out
+
+    def diagnostics(self, start=0, end=0, probs=(0.05, 0.5, 0.975), conf=0.95, form=abi.PSRF_REFERENCE,
+                    phi=False):
+        """summary + gelman of the last run's samples, on the device
+        (ggdmc_handle_diagnostics): {"subj": {...} [S][P], "phi": {...} [2P]}
+        with mean, sd, naive_se, ts_se, quantiles [..][n_prob], psrf [..][2]."""
+        pr = np.ascontiguousarray(probs, np.float64)
+        levels = [("subj", self.batch.n_subject, self.model.n_par)]
+        if phi:
+            levels.append(("phi", 1, 2 * self.model.n_par))
+        outs, structs = {}, []
+        for name, L, P in levels:
+            o = {k: np.full((L, P), np.nan) for k in ("mean", "sd", "naive_se", "ts_se")}
+            o["quantiles"] = np.full((L, P, len(pr)), np.nan)
+            o["psrf"] = np.full((L, P, 2), np.nan)
+            outs[name] = o
+            structs.append(abi.Diag(*[abi.dptr(o[k]) for k in ("mean", "sd", "naive_se", "ts_se", "quantiles",
+                                                                "psrf")]))
+        ph = C.byref(structs[1]) if phi else None
+        check(lib().ggdmc_handle_diagnostics(self.h, start, end, abi.dptr(pr) if len(pr) else None, len(pr),
+                                             conf, form, C.byref(structs[0]), ph))
+        if phi:
+            outs["phi"] = {k: v[0] for k, v in outs["phi"].items()}
+        return outs
 
     def trial_logdens(self, theta, precision=abi.FP64):
         """theta [S][P] -> per-trial log densities [N]."""

@@ -292,6 +292,44 @@ ggdmc_status ggdmc_handle_summary(ggdmc_handle *h, int32_t start, double *mean,
                                   double *sd, double *psrf, double *phi_mean,
                                   double *phi_sd, double *phi_psrf);
 
+/* The full summary and gelman diagnostics of the samples the last
+ * ggdmc_handle_run left on the device, computed there.  Per level (subject
+ * or phi) and parameter, over the iterations [start, end) of every chain
+ * (end <= 0: nmc; R's start is 1-based and its end inclusive):
+ *   mean, sd    summary's "Mean" and "SD" over all chains and iterations
+ *   naive_se    "Naive SE" = sqrt(var / niter * nchain), the reference's
+ *               formula (R/model-class.R:410)
+ *   ts_se       "Time-series SE" = sqrt(mean over chains of safespec0 /
+ *               niter * nchain): spectrum0_ar's AR spectral density at zero
+ *               (R/model-class.R:257-281; Yule-Walker, order by AIC up to
+ *               min(n - 1, floor(10 log10 n)))
+ *   quantiles   [n_prob] per parameter, of type 7 (matrixStats::rowQuantiles)
+ *   psrf        [2] per parameter: gelman's "Point est." and "Upper C.I."
+ *               at level conf (R/model-class.R:1590-1616, 1677-1683)
+ * Each pointer may be NULL (not computed).  probs (host) default in R to
+ * 0.05, 0.5, 0.975; n_prob is 0 or 2..16 ("prob must be more than one
+ * element").  psrf_form GGDMC_PSRF_REFERENCE is the reference's own form
+ * (the variance of each row of W stands for the variance of the chains'
+ * variances, no W-B covariance term; NaN for one parameter; needs n_par <= 64
+ * at that level), GGDMC_PSRF_CODA Brooks & Gelman's as coda computes it.
+ * GGDMC_ERR_ARG without stored samples, for fewer than 2 iterations, more
+ * than 2.5e6 iterations, psrf with fewer than 3 chains ("Minimum three
+ * chains needed"), or conf outside (0, 1). */
+#define GGDMC_PSRF_REFERENCE 0
+#define GGDMC_PSRF_CODA 1
+typedef struct {
+    double *mean;              /* [n_level][n_par]         */
+    double *sd;                /* [n_level][n_par]         */
+    double *naive_se;          /* [n_level][n_par]         */
+    double *ts_se;             /* [n_level][n_par]         */
+    double *quantiles;         /* [n_level][n_par][n_prob] */
+    double *psrf;              /* [n_level][n_par][2]      */
+} ggdmc_diag;
+
+ggdmc_status ggdmc_handle_diagnostics(ggdmc_handle *h, int32_t start, int32_t end,
+                                      const double *probs, int32_t n_prob, double conf,
+                                      int32_t psrf_form, ggdmc_diag *subj, ggdmc_diag *phi);
+
 /* Run on a resident handle: level layout as ggdmc_run (phi_state == NULL
  * runs the subjects as independent fits, like ggdmc_run_subjects). */
 ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg,

@@ -1,4 +1,5 @@
-// Host entry points over ggdmc_gb300/csrc/dfloat.h for tests/test_dfloat.py:
+// Host entry points over ggdmc_gb300/csrc/dfloat.h and fquantile.h for
+// tests/test_dfloat.py and tests/test_diagnostics.py:
 // each takes n doubles, splits them to hi + lo, applies one double-float
 // function and writes the result back as a double.
 #include "dfloat.h"
@@ -39,4 +40,11 @@ void dfc_add(const double *a, const double *b, double *y, int n)
 {
     for (int i = 0; i < n; ++i) y[i] = df_to_double(df_add(df_from_double(a[i]), df_from_double(b[i])));
 }
+}
+
+#include "fquantile.h"
+
+extern "C" void fqc_quantile(const double *p, const double *d1, const double *d2, double *y, int n)
+{
+    for (int i = 0; i < n; ++i) y[i] = f_quantile(p[i], d1[i], d2[i]);
 }
