@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_TIMEOUT",
                 4: "ERR_NUMERIC", 5: "ERR_NOMEM"}
 
 MODEL_LBA, MODEL_DDM = 0, 1
-FP64, MIXED, FP64_PLAIN = 0, 1, 2
+FP64, MIXED, FP64_PLAIN, MIXED_SUMS = 0, 1, 2, 3
 PRIOR_TNORM, PRIOR_UNIF = 1, 6
 FLAG_L2_FLUSH = 1
 

@@ -147,7 +147,8 @@ __device__ __forceinline__ double lba_logdens64(double t, const int *ents, int K
 //
 // Per proposal and accumulator tuple (the host builds them in FP64):
 struct Ent32 {
-    float4 a;   // beta_h, betam_h, kappa_h, hA_h      hA = A / (2 s)
+    float4 a;   // beta_h, betam_h, kappa_h, hA_h      hA = A / (2 s); the density forms
+                //                                      czm from cz and hA, not from betam
     float4 b;   // beta_l, betam_l, kappa_l, hA_l      (low parts)
     float4 c;   // g_h, g_l, q_h, q_l
 };
@@ -181,6 +182,17 @@ __device__ __forceinline__ void zdf(float bh, float bl, float uh, float ul, floa
     float s, e;
     two_diff(p, kh, s, e);
     const float l = e + (pe - kl);
+    zh = s + l;
+    zl = l - (zh - s);
+}
+
+// czm = cz - 2h = betam u - kappa from cz and h = hA u (each hi + lo),
+// normalised: betam = beta - 2 hA, so the second product is not needed
+__device__ __forceinline__ void zlower(float czh, float czl, float h, float hc, float &zh, float &zl)
+{
+    float s, e;
+    two_diff(czh, 2.f * h, s, e);
+    const float l = e + (czl - 2.f * hc);
     zh = s + l;
     zl = l - (zh - s);
 }
@@ -222,8 +234,8 @@ __device__ __forceinline__ bool winner_br(const Ent32 &P, float uh, float ul, fl
 {
     float czh, czl, cmh, cml;
     zdf(P.a.x, P.b.x, uh, ul, P.a.z, P.b.z, czh, czl);
-    zdf(P.a.y, P.b.y, uh, ul, P.a.z, P.b.z, cmh, cml);
     const float h = P.a.w * uh, hc = fmaf(P.a.w, ul, P.b.w * uh);
+    zlower(czh, czl, h, hc, cmh, cml);
     const float mh = czh - h, ml = (czl - hc) + ((czh - mh) - h);
     float ref;   // the reference form's FP64 rounding in its bracket
     if (h * fmaxf(1.f, fabsf(mh)) < kGlMax) {
@@ -260,8 +272,8 @@ __device__ __forceinline__ bool loser_s(const Ent32 &P, float th, float tl, floa
 {
     float czh, czl, cmh, cml;
     zdf(P.a.x, P.b.x, uh, ul, P.a.z, P.b.z, czh, czl);
-    zdf(P.a.y, P.b.y, uh, ul, P.a.z, P.b.z, cmh, cml);
     const float h = P.a.w * uh, hc = fmaf(P.a.w, ul, P.b.w * uh);
+    zlower(czh, czl, h, hc, cmh, cml);
     const float mh = czh - h, ml = (czl - hc) + ((czh - mh) - h);
     float terms;   // the reference's survivor sums terms of this size, scaled 1/(2h)
     bool ok;

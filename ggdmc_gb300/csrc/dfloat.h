@@ -132,6 +132,7 @@ GG_HD dfl df_exp(dfl x)
                                 {2.7557318844628753e-06f, 3.793571224297229e-14f},
                                 {2.755731998149713e-07f, -7.575112209051195e-15f}};
     dfl p = dfl{c[10][0], c[10][1]};
+#pragma unroll
     for (int i = 9; i >= 0; --i) p = df_add(df_mul(p, r), dfl{c[i][0], c[i][1]});
     return df_scale(p, (int)k);
 }
@@ -157,6 +158,7 @@ GG_HD dfl df_log(dfl x)
                                {0.1111111119389534f, -8.278422947149977e-10f},
                                {0.09090909361839294f, -2.709302115988521e-09f}};
     dfl p = dfl{c[5][0], c[5][1]};
+#pragma unroll
     for (int i = 4; i >= 0; --i) p = df_add(df_mul(p, s2), dfl{c[i][0], c[i][1]});
     const dfl lm = df_mul_f(df_mul(p, s), 2.f);
     return df_add(df_mul_f(dfl{kDfLn2H, kDfLn2L}, (float)e), lm);
@@ -188,9 +190,13 @@ GG_HD dfl df_qtail(dfl x)
                                 {22.7136287689209f, 6.636840055307403e-08f}};
     const dfl xc = (x.h > 14.f) ? dfl{14.f, 0.f} : x;
     const dfl t = df_mul(xc, dfl{0.0714285746216774f, -3.19310600183087e-09f});   // x / 14
+    // the two Horner chains are independent; unrolled, the tables become immediates
     dfl p = dfl{P[8][0], P[8][1]}, q = dfl{Q[9][0], Q[9][1]};
-    for (int i = 7; i >= 0; --i) p = df_add(df_mul(p, t), dfl{P[i][0], P[i][1]});
-    for (int i = 8; i >= 0; --i) q = df_add(df_mul(q, t), dfl{Q[i][0], Q[i][1]});
+#pragma unroll
+    for (int i = 8; i >= 0; --i) {
+        if (i < 8) p = df_add(df_mul(p, t), dfl{P[i][0], P[i][1]});
+        q = df_add(df_mul(q, t), dfl{Q[i][0], Q[i][1]});
+    }
     const dfl mills = df_div(p, q);
     // phi(x) = exp(-x^2 / 2) / sqrt(2 pi), x^2 exactly as hi + lo
     const dfl x2 = df_mul(x, x);

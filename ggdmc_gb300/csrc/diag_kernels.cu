@@ -332,7 +332,9 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_quant(const double *smp, 
         const double h = (N - 1) * probs[i];
         const double g = h - floor(h);
         const double xlo = dval(prefix[2 * i]), xhi = dval(prefix[2 * i + 1]);
-        out[(size_t)blockIdx.x * n_prob + i] = (g == 0.0 || xhi == xlo) ? xlo : (1.0 - g) * xlo + g * xhi;
+        // (1 - g) xlo + g xhi rounded term by term, as R and the host form it (no FMA)
+        out[(size_t)blockIdx.x * n_prob + i] =
+            (g == 0.0 || xhi == xlo) ? xlo : __dadd_rn(__dmul_rn(1.0 - g, xlo), __dmul_rn(g, xhi));
     }
 }
 

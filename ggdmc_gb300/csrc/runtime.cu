@@ -170,6 +170,7 @@ struct ggdmc_handle {
     int S = 0;
     int last_nmc = 0, last_C = 0, last_P = 0, last_Pphi = 0, last_S = 0;   // samples left by the last run
     std::vector<int64_t> h_offs;
+    std::vector<int64_t> perm;     // stored trial j is data trial perm[j] (upload_data)
     DevBuf<int64_t> offs;
     DevBuf<double> rt64;
     DevBuf<float2> rt32;
@@ -409,28 +410,41 @@ ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
         if (offs[s + 1] < offs[s]) return fail(GGDMC_ERR_ARG, "offsets must be non-decreasing");
     const int64_t N = offs[S];
     if (N > 0 && (!d->rt || !d->cell)) return fail(GGDMC_ERR_ARG, "rt / cell missing");
+    std::vector<int32_t> cnt((size_t)std::max(S, 1) * h->n_cell, 0);
+    for (int64_t i = 0; i < N; ++i) {
+        if (!std::isfinite(d->rt[i])) return fail(GGDMC_ERR_ARG, "non-finite RT in data");
+        if (d->cell[i] < 0 || d->cell[i] >= h->n_cell) return fail(GGDMC_ERR_ARG, "cell index out of range");
+    }
+    // Each subject's trials are stored by (cell, RT): a warp's 32 trials then
+    // mostly share a cell (one table entry set, read as a shared-memory
+    // broadcast) and a response-time range (the same branches of the FP32
+    // density).  A subject's sums do not depend on the order beyond
+    // rounding; perm maps a stored trial back to its place in the data.
+    std::vector<int64_t> perm(N);
+    for (int s = 0; s < S; ++s) {
+        int64_t *b = perm.data() + offs[s], *e = perm.data() + offs[s + 1];
+        std::iota(b, e, offs[s]);
+        std::stable_sort(b, e, [&](int64_t x, int64_t y) {
+            return d->cell[x] != d->cell[y] ? d->cell[x] < d->cell[y] : d->rt[x] < d->rt[y];
+        });
+        for (int64_t *q = b; q < e; ++q) ++cnt[(size_t)s * h->n_cell + d->cell[*q]];
+    }
+    std::vector<double> r64(N);
     std::vector<float2> r32(N);
     std::vector<uint16_t> c16(N);
-    std::vector<int32_t> cnt((size_t)std::max(S, 1) * h->n_cell, 0);
-    for (int s = 0; s < S; ++s)
-        for (int64_t i = offs[s]; i < offs[s + 1]; ++i) {
-            const int c = d->cell[i];
-            if (c >= 0 && c < h->n_cell) ++cnt[(size_t)s * h->n_cell + c];
-        }
-    for (int64_t i = 0; i < N; ++i) {
-        const double rt = d->rt[i];
-        if (!std::isfinite(rt)) return fail(GGDMC_ERR_ARG, "non-finite RT in data");
-        const int c = d->cell[i];
-        if (c < 0 || c >= h->n_cell) return fail(GGDMC_ERR_ARG, "cell index out of range");
+    for (int64_t j = 0; j < N; ++j) {
+        const double rt = d->rt[perm[j]];
         const float hi = (float)rt;
-        r32[i] = make_float2(hi, (float)(rt - (double)hi));
-        c16[i] = (uint16_t)c;
+        r64[j] = rt;
+        r32[j] = make_float2(hi, (float)(rt - (double)hi));
+        c16[j] = (uint16_t)d->cell[perm[j]];
     }
     h->S = S;
     h->h_offs = offs;
+    h->perm = std::move(perm);
     cudaStream_t st = h->stream;
     CU(h->offs.upload(offs.data(), offs.size(), st));
-    CU(h->rt64.upload(d->rt, N, st));
+    CU(h->rt64.upload(r64.data(), N, st));
     CU(h->rt32.upload(r32.data(), N, st));
     CU(h->cell.upload(c16.data(), N, st));
     CU(h->cell_cnt.upload(cnt.data(), cnt.size(), st));
@@ -1269,7 +1283,7 @@ static RunDev loglik_desc(ggdmc_handle *h, int prec)
     RunDev r{};
     r.P = h->n_par;
     r.S = h->S;
-    r.prec = (prec == GGDMC_MIXED) ? PREC_MIXED : PREC_FP64;
+    r.prec = (prec == GGDMC_MIXED || prec == GGDMC_MIXED_SUMS) ? PREC_MIXED : PREC_FP64;
     r.m = h->dev_model();
     r.offs = h->offs.p; r.rt64 = h->rt64.p; r.rt32 = h->rt32.p; r.cell = h->cell.p;
     r.cell_cnt = h->cell_cnt.p;
@@ -1469,8 +1483,12 @@ ggdmc_status ggdmc_trial_logdens(ggdmc_handle *h, const double *theta, int32_t p
     CU(h->io_b.alloc(std::max<size_t>(N, 1)));
     RunDev r = loglik_desc(h, precision);
     CU(launch_trial_logdens(r, h->io_a.p, h->io_b.p, h->stream));
-    if (N) CU(cudaMemcpyAsync(out, h->io_b.p, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
-    return wait_stream(h->stream);
+    std::vector<double> dev(N);
+    if (N) CU(cudaMemcpyAsync(dev.data(), h->io_b.p, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+    ggdmc_status ws = wait_stream(h->stream);
+    if (ws) return ws;
+    for (size_t j = 0; j < N; ++j) out[h->perm[j]] = dev[j];   // back to the data's trial order
+    return GGDMC_OK;
 }
 
 ggdmc_status ggdmc_logprior(const ggdmc_prior *prior, const double *theta, int32_t n, double *out)

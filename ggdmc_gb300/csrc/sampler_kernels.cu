@@ -513,61 +513,20 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
     for (int g = 0; g < ng; ++g) out[g] = block_sum(acc[g] + ((double)ks[g] - (double)kc[g]), sm.red);
 }
 
-// Sums of a group of ng (<= G) proposals over the CTA, every thread gets
-// out[g] = sum d + sum (h - c) + ln 2 sum e: d the FP64 parts (the per-cell
-// log g constants and FP64 re-evaluations), h - c the Kahan-compensated FP32
-// sums of the mantissa logs (reduced as double-float pairs), e the binary
-// exponents (exact).  One exchange through shared memory, warp g reducing
-// proposal g; the order of every sum is fixed.
-template <int G>
-__device__ __forceinline__ void block_sum_mixed(const double (&d)[G], const float (&h)[G], const float (&c)[G],
-                                                const int (&e)[G], int ng, double *red, double *out)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nw = (blockDim.x + 31) >> 5;
-    double *rd = red;                               // [G][32]
-    float *rf = (float *)(red + G * 32);            // [G][32] (h, l)
-    int *ri = (int *)(red + G * 64);                // [G][32]
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-        if (g >= ng) break;
-        double dd = d[g];
-        float hh = h[g], ll = -c[g];
-        int ee = e[g];
-        for (int o = 16; o > 0; o >>= 1) {
-            dd += __shfl_down_sync(0xffffffffu, dd, o);
-            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
-            ff_add(hh, ll, h2, l2);
-            ee += __shfl_down_sync(0xffffffffu, ee, o);
-        }
-        if (lane == 0) {
-            rd[g * 32 + wid] = dd;
-            rf[2 * (g * 32 + wid)] = hh;
-            rf[2 * (g * 32 + wid) + 1] = ll;
-            ri[g * 32 + wid] = ee;
-        }
-    }
-    __syncthreads();
-    double *res = red + G * 96;
-    for (int g = wid; g < ng; g += nw) {
-        double dd = (lane < nw) ? rd[g * 32 + lane] : 0.0;
-        float hh = (lane < nw) ? rf[2 * (g * 32 + lane)] : 0.f;
-        float ll = (lane < nw) ? rf[2 * (g * 32 + lane) + 1] : 0.f;
-        int ee = (lane < nw) ? ri[g * 32 + lane] : 0;
-        for (int o = 16; o > 0; o >>= 1) {
-            dd += __shfl_down_sync(0xffffffffu, dd, o);
-            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
-            ff_add(hh, ll, h2, l2);
-            ee += __shfl_down_sync(0xffffffffu, ee, o);
-        }
-        if (lane == 0) res[g] = dd + ((double)hh + (double)ll) + kLn2 * (double)ee;
-    }
-    __syncthreads();
-    for (int g = 0; g < ng; ++g) out[g] = res[g];
-    __syncthreads();
-}
+// Warp partials of group_loglik's FP32 pass, in sm.red: per proposal g and
+// warp w the double-float sum (h, l) of the trials' mantissa logs (Kahan sum
+// and compensation of each thread, reduced over the warp), the sum of their
+// binary exponents and the count of trials left to FP64; then per proposal
+// the result and its FP64 count.
+struct WarpPart {
+    float h, l;
+    int e, nf;
+};
+constexpr int kWpDoubles = kGroup * 32 * (int)(sizeof(WarpPart) / sizeof(double));
+static_assert(kWpDoubles + 2 * kGroup <= kRedDoubles, "sm.red holds the warp partials and the results");
+__device__ __forceinline__ WarpPart *warp_parts(const SubSmem &sm) { return reinterpret_cast<WarpPart *>(sm.red); }
+__device__ __forceinline__ double *group_res(const SubSmem &sm) { return sm.red + kWpDoubles; }
+__device__ __forceinline__ int *group_nf(const SubSmem &sm) { return reinterpret_cast<int *>(sm.red + kWpDoubles + kGroup); }
 
 // Kahan-compensated FP32 accumulation (sum s, compensation c)
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
@@ -580,20 +539,20 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 
 // The FP32 pass of group_loglik over trials [base, base + n) for K
 // accumulators (K = 0: the design's count at run time), one proposal at a
-// time, so a thread holds one proposal's sums; the subject's trial data is
-// read once per proposal (it stays in L1).  A trial the FP32 form declines
-// is listed for FP64.
+// time: a thread holds one proposal's sums, which its warp reduces into
+// warp_parts once the proposal's trials are done (no per-proposal arrays;
+// every sum in a fixed order).  The subject's trial data is read once per
+// proposal (it stays in L1).  A trial the FP32 form declines is listed for
+// FP64.
 template <int K>
-__device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, int n, const SubSmem &sm,
-                                                 const bool (&ok)[kGroup], float (&ks)[kGroup],
-                                                 float (&kc)[kGroup], int (&es)[kGroup], int (&nfb)[kGroup])
+__device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, int n, const SubSmem &sm, int ng)
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0, KR = r.m.n_acc;
-    // not unrolled: one copy of the density loop, and the per-proposal sums
-    // (stored once per proposal) need no registers across it
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    WarpPart *wp = warp_parts(sm);
 #pragma unroll 1
-    for (int g = 0; g < kGroup; ++g) {
-        if (!ok[g]) continue;                       // uniform over the block
+    for (int g = 0; g < ng; ++g) {
+        if (sm.flag[g] != 0) continue;              // uniform over the block
         const Ent32 *E = sm.e32 + g * NE;
         const float2 *T0 = sm.t032 + g * NT;
         float s = 0.f, cmp = 0.f;
@@ -621,10 +580,15 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
                 if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
             }
         }
-        ks[g] = s;
-        kc[g] = cmp;
-        es[g] = e;
-        nfb[g] = nf;
+        float hh = s, ll = -cmp;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
+            ff_add(hh, ll, h2, l2);
+            e += __shfl_down_sync(0xffffffffu, e, o);
+            nf += __shfl_down_sync(0xffffffffu, nf, o);
+        }
+        if (lane == 0) wp[g * 32 + wid] = WarpPart{hh, ll, e, nf};
     }
 }
 
@@ -636,9 +600,10 @@ constexpr int kAnyModel = 0, kLbaOnly = 1, kDdmOnly = 2, kLba4 = 3;
 // Log-likelihood sums of the subject's trials for the ng (<= kGroup)
 // proposals loaded in sm, on the whole CTA; out[g] valid on all threads.
 // MIXED: a trial's log density is log g_w (in FP64, once per cell through
-// the subject's cell counts) + e ln 2 + log m from lba_ld32; FP64 tables are
-// built only for a proposal some trial of which needs the FP64 form, and only
-// those trials use it.
+// the subject's cell counts) + e ln 2 + log m from lba_ld32; warp g combines
+// proposal g's warp partials and its per-cell constant.  FP64 tables are
+// built only for a proposal some trial of which needs the FP64 form, and
+// only those trials use it.
 template <int MODEL = kAnyModel>
 __device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool mixed, double *out)
 {
@@ -668,61 +633,75 @@ __device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool m
     }
     if (threadIdx.x == 0) *sm.fbn = 0;
     __syncthreads();
-    bool ok[kGroup];
-    float ks[kGroup], kc[kGroup];
-    int es[kGroup], nfb[kGroup];
-    double d[kGroup];
-#pragma unroll
-    for (int g = 0; g < kGroup; ++g) {
-        ok[g] = g < ng && sm.flag[g] == 0;
-        ks[g] = 0.f; kc[g] = 0.f; es[g] = 0; nfb[g] = 0; d[g] = 0.0;
-    }
     switch (MODEL == kLba4 ? 4 : K) {
-    case 2: if constexpr (MODEL != kLba4) lba_group_loop32<2>(r, base, n, sm, ok, ks, kc, es, nfb); break;
-    case 3: if constexpr (MODEL != kLba4) lba_group_loop32<3>(r, base, n, sm, ok, ks, kc, es, nfb); break;
-    case 4: lba_group_loop32<4>(r, base, n, sm, ok, ks, kc, es, nfb); break;
-    default: if constexpr (MODEL != kLba4) lba_group_loop32<0>(r, base, n, sm, ok, ks, kc, es, nfb); break;
+    case 2: if constexpr (MODEL != kLba4) lba_group_loop32<2>(r, base, n, sm, ng); break;
+    case 3: if constexpr (MODEL != kLba4) lba_group_loop32<3>(r, base, n, sm, ng); break;
+    case 4: lba_group_loop32<4>(r, base, n, sm, ng); break;
+    default: if constexpr (MODEL != kLba4) lba_group_loop32<0>(r, base, n, sm, ng); break;
     }
-    // log g of each trial's winning tuple, by cell: sum over cells of n_c log g
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const WarpPart *wp = warp_parts(sm);
+    double *res = group_res(sm);
+    int *gnf = group_nf(sm);
     const int32_t *cnt = r.cell_cnt + (size_t)l * r.m.n_cell;
-    for (int c = threadIdx.x; c < r.m.n_cell; c += blockDim.x) {
-        const int nc = cnt[c];
-        if (!nc) continue;
-        const int u = sm.cent[c * K];
-#pragma unroll
-        for (int g = 0; g < kGroup; ++g)
-            if (ok[g]) d[g] += (double)nc * sm.lg[g * NE + u];
-    }
-    bool anyfb = false;
-#pragma unroll
-    for (int g = 0; g < kGroup; ++g)
-        if (g < ng) anyfb |= nfb[g] > 0 || sm.flag[g] != 0;
-    if (__syncthreads_or(anyfb)) {
-        // FP64 for the listed trials (their log g was counted above, so it
-        // is taken back out), or for every trial of a proposal outside the
-        // FP32 form's domain
-#pragma unroll
-        for (int g = 0; g < kGroup; ++g) {
-            if (g >= ng) break;
-            const bool usable = sm.flag[g] == 0;
-            if (!__syncthreads_or(nfb[g] > 0 || !usable)) continue;
-            build_tables64(r, sm, sm.theta + g * kMaxTheta);
-            if (r.stats) {
-                const int nf = usable ? nfb[g] : (threadIdx.x == 0 ? n : 0);
-                if (nf) atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)nf);
+    for (int g = wid; g < ng; g += nw) {
+        float hh = 0.f, ll = 0.f;
+        int ee = 0, nf = 0;
+        double dc = 0.0;
+        if (sm.flag[g] == 0) {
+            if (lane < nw) {
+                const WarpPart p = wp[g * 32 + lane];
+                hh = p.h;
+                ll = p.l;
+                ee = p.e;
+                nf = p.nf;
             }
+            // log g of each trial's winning tuple, by cell: sum over cells of n_c log g
+            for (int c = lane; c < r.m.n_cell; c += 32) {
+                const int nc = cnt[c];
+                if (nc) dc += (double)nc * sm.lg[g * NE + sm.cent[c * K]];
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
+            ff_add(hh, ll, h2, l2);
+            ee += __shfl_down_sync(0xffffffffu, ee, o);
+            nf += __shfl_down_sync(0xffffffffu, nf, o);
+            dc += __shfl_down_sync(0xffffffffu, dc, o);
+        }
+        if (lane == 0) {
+            res[g] = dc + ((double)hh + (double)ll) + kLn2 * (double)ee;
+            gnf[g] = nf;
+        }
+    }
+    __syncthreads();
+    bool anyfb = false;
+    for (int g = 0; g < ng; ++g) anyfb |= gnf[g] > 0 || sm.flag[g] != 0;
+    if (anyfb) {
+        // FP64 for the listed trials (their log g was counted above, so it is
+        // taken back out), or for every trial of a proposal outside the FP32
+        // form's domain
+        for (int g = 0; g < ng; ++g) {
+            const bool usable = sm.flag[g] == 0;
+            if (usable && gnf[g] == 0) continue;    // uniform over the block
+            build_tables64(r, sm, sm.theta + g * kMaxTheta);
+            if (r.stats && threadIdx.x == 0)
+                atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)(usable ? gnf[g] : n));
             __syncthreads();
             const int fbn = *sm.fbn;
+            double acc = 0.0;
             if (!usable) {
-                for (int i = threadIdx.x; i < n; i += blockDim.x) d[g] += trial64(r, sm, base + i, r.cell[base + i], K);
+                for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
             } else if (fbn <= kFbCap) {
                 for (int q = threadIdx.x; q < fbn; q += blockDim.x) {
                     const int e = sm.fb[q];
                     if ((e & 3) != g) continue;
                     const int i = e >> 2, c = r.cell[base + i];
-                    d[g] += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
+                    acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
                 }
-            } else if (nfb[g] > 0) {
+            } else {
                 for (int i = threadIdx.x; i < n; i += blockDim.x) {
                     const int c = r.cell[base + i];
                     int ex;
@@ -730,13 +709,16 @@ __device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool m
                     if (lba_ld32_n(r.rt32[base + i], sm.t032[g * NT + sm.ct0[c]], sm.cent + c * K, K, sm.e32 + g * NE,
                                    ex, lm))
                         continue;
-                    d[g] += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
+                    acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
                 }
             }
+            const double tot = block_sum(acc, sm.red);      // red[0..32]: the warp partials are consumed
+            if (threadIdx.x == 0) res[g] += tot;
             __syncthreads();
         }
     }
-    block_sum_mixed(d, ks, kc, es, ng, sm.red, out);
+    for (int g = 0; g < ng; ++g) out[g] = res[g];
+    __syncthreads();
 }
 
 // Evaluate the log-likelihoods of proposal slots `slots[0..m)` of level l on

@@ -50,7 +50,7 @@ enum { GGDMC_MODEL_LBA = 0, GGDMC_MODEL_DDM = 1 };
  *                 priors and the Metropolis difference in FP64.
  *  FP64_PLAIN  -- double throughout, one launch per subject per pass: the
  *                 plain GPU form the batched kernels are measured against. */
-enum { GGDMC_FP64 = 0, GGDMC_MIXED = 1, GGDMC_FP64_PLAIN = 2 };
+enum { GGDMC_FP64 = 0, GGDMC_MIXED = 1, GGDMC_FP64_PLAIN = 2, GGDMC_MIXED_SUMS = 3 };
 
 /* ggdmc_de_config.flags: flush L2 between iterations and report in
  * ggdmc_run_stats.sweep_ms only the iterations' own kernel time (benchmarks). */
@@ -230,7 +230,12 @@ ggdmc_status ggdmc_destroy(ggdmc_handle *h);
 
 /* Per-subject log-likelihood sums of n_theta parameter vectors per subject:
  * theta [n_subject][n_theta][n_par] -> out [n_subject][n_theta].
- * This is LPtr->sumloglike (called at src/de.cpp:145,187,604,653) batched. */
+ * This is LPtr->sumloglike (called at src/de.cpp:145,187,604,653) batched.
+ * precision GGDMC_MIXED adds an FP64 pass over the sums whose FP32 error
+ * could exceed 1e-6 of their size (|sum| < 1.2 sqrt(N) + 0.03 N for N
+ * trials: sums near zero), so that every sum is within 1e-6 relative of the
+ * FP64 one; GGDMC_MIXED_SUMS returns the FP32 sums as the sampler forms
+ * them, without that pass (likelihood calls only). */
 ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta,
                           int32_t precision, double *out);
 

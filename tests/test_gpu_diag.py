@@ -92,7 +92,7 @@ def test_diagnostics_argument_errors():
     th, _ = synth.start_states(w, 3, np.random.default_rng(2))
     lp = np.stack([gpu.logprior(w.p_prior, th[s]) for s in range(2)])
     ll = h.loglik(th, abi.FP64)
-    cfg = abi.DEConfigPy(nchain=3, nparameter=2 * w.model.n_par, nmc=20, thin=1, seed=1)
+    cfg = abi.DEConfigPy(nchain=3, nparameter=w.model.n_par, nmc=20, thin=1, seed=1)
     h.run(cfg, w.p_prior, th, lp, ll)
     with pytest.raises(gpu.GGDMCError, match="more than one element"):
         h.diagnostics(probs=(0.5,))
