@@ -70,7 +70,9 @@ class RunStats(C.Structure):
     _fields_ = [("proposals", C.c_int64), ("accepts", C.c_int64), ("migrations", C.c_int64),
                 ("reevaluations", C.c_int64), ("kernel_launches", C.c_int64),
                 ("trial_evals", C.c_int64), ("iterations", C.c_int64), ("sweep_ms", C.c_double),
-                ("resolve_rounds", C.c_int64), ("variants", C.c_int64), ("fallbacks", C.c_int64)]
+                ("resolve_rounds", C.c_int64), ("variants", C.c_int64), ("fallbacks", C.c_int64),
+                ("setup_ms", C.c_double), ("capture_ms", C.c_double), ("run_ms", C.c_double),
+                ("copyout_ms", C.c_double)]
 
 
 def dptr(a: np.ndarray):

@@ -482,8 +482,15 @@ struct RunArgs {
     int n_row;
 };
 
+static double ms_since(std::chrono::steady_clock::time_point t0)
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
 {
+    const auto t_in = std::chrono::steady_clock::now();
+    double t_setup = 0.0, t_capture = 0.0, t_run = 0.0;
     ggdmc_status s;
     if ((s = check_cfg(a.cfg))) return s;
     const ggdmc_de_config &c = *a.cfg;
@@ -813,6 +820,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         };
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
+        t_setup = ms_since(t_in);
+        const auto t_cap = std::chrono::steady_clock::now();
         CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaError_t ce = cudaSuccess;
         launches_per_iter = 0;
@@ -930,6 +939,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             return GGDMC_OK;
         };
 
+        t_capture = ms_since(t_cap);
+        const auto t_rep = std::chrono::steady_clock::now();
         if (!flush) CU(cudaEventRecord(ev_a[per_graph], st));
         while (done + per_graph <= n_iter && !ws) {
             cudaError_t e = cudaGraphLaunch(exec, st);
@@ -988,6 +999,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             if (flush && !ws) cudaMemsetAsync(h->flushbuf.p, 0, kFlushBytes, st);
         }
         launches += n_iter * per_iter;
+        t_run = ms_since(t_rep);
         cudaGraphExecDestroy(exec);
         cudaGraphDestroy(graph);
         cleanup_events();
@@ -996,6 +1008,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     }
 
     // ---- copy back: final state and samples
+    if (n_iter == 0) t_setup = ms_since(t_in);
+    const auto t_out = std::chrono::steady_clock::now();
     if (S > 0) {
         std::vector<double> buf((size_t)S * C * P), b1((size_t)S * C), b2((size_t)S * C);
         CU(cudaMemcpyAsync(buf.data(), h->th.p, sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, st));
@@ -1062,6 +1076,10 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         a.stats->fallbacks = (int64_t)hs[ST_FALLBACKS];
         a.stats->iterations = n_iter;
         a.stats->sweep_ms = sweep_ms;
+        a.stats->setup_ms = t_setup;
+        a.stats->capture_ms = t_capture;
+        a.stats->run_ms = t_run;
+        a.stats->copyout_ms = ms_since(t_out);
     }
     return GGDMC_OK;
 }
@@ -1205,6 +1223,28 @@ ggdmc_status ggdmc_destroy(ggdmc_handle *h)
     return GGDMC_OK;
 }
 
+// A one-shot call: a handle for the call's design and trials, the run, the
+// release; the handle's creation counts into setup_ms and its release into
+// copyout_ms.
+static ggdmc_status run_oneshot(const ggdmc_model *model, const ggdmc_data *data, const RunArgs &a)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    ggdmc_handle *h = nullptr;
+    ggdmc_status s = make_handle(model, data, &h);
+    if (s) return s;
+    const double t_make = ms_since(t0);
+    s = run_impl(h, a);
+    const std::string keep = g_err;
+    const auto t1 = std::chrono::steady_clock::now();
+    ggdmc_destroy(h);
+    g_err = keep;
+    if (a.stats && !s) {
+        a.stats->setup_ms += t_make;
+        a.stats->copyout_ms += ms_since(t1);
+    }
+    return s;
+}
+
 ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg, const ggdmc_prior *p_prior,
                               const ggdmc_prior *h_prior, ggdmc_chain_state *phi_state,
                               ggdmc_chain_state *subj_state, const double *draws,
@@ -1221,16 +1261,9 @@ ggdmc_status ggdmc_run_subjects(const ggdmc_de_config *cfg, const ggdmc_model *m
                                 ggdmc_chain_state *state, const double *draws, ggdmc_samples *out,
                                 ggdmc_run_stats *stats)
 {
-    ggdmc_handle *h = nullptr;
-    ggdmc_status s = make_handle(model, data, &h);
-    if (s) return s;
     RunArgs a{RK_SUBJECTS, cfg, p_prior, nullptr, nullptr, state, draws, nullptr, out, stats,
               nullptr, 0};
-    s = run_impl(h, a);
-    const std::string keep = g_err;
-    ggdmc_destroy(h);
-    g_err = keep;
-    return s;
+    return run_oneshot(model, data, a);
 }
 
 ggdmc_status ggdmc_run_subject(const ggdmc_de_config *cfg, const ggdmc_model *model,
@@ -1249,16 +1282,9 @@ ggdmc_status ggdmc_run(const ggdmc_de_config *cfg, const ggdmc_model *model, con
                        const double *draws, ggdmc_samples *phi_out, ggdmc_samples *subj_out,
                        ggdmc_run_stats *stats)
 {
-    ggdmc_handle *h = nullptr;
-    ggdmc_status s = make_handle(model, data, &h);
-    if (s) return s;
     RunArgs a{RK_HIER, cfg, p_prior, h_prior, phi_state, subj_state, draws, phi_out, subj_out,
               stats, nullptr, 0};
-    s = run_impl(h, a);
-    const std::string keep = g_err;
-    ggdmc_destroy(h);
-    g_err = keep;
-    return s;
+    return run_oneshot(model, data, a);
 }
 
 ggdmc_status ggdmc_run_hyper(const ggdmc_de_config *cfg, const double *hyper_data, int32_t n_row,
@@ -1266,16 +1292,9 @@ ggdmc_status ggdmc_run_hyper(const ggdmc_de_config *cfg, const double *hyper_dat
                              ggdmc_chain_state *state, const double *draws, ggdmc_samples *out,
                              ggdmc_run_stats *stats)
 {
-    ggdmc_handle *h = nullptr;
-    ggdmc_status s = make_handle(nullptr, nullptr, &h);
-    if (s) return s;
     RunArgs a{RK_HYPER, cfg, p_prior, h_prior, state, nullptr, draws, out, nullptr, stats,
               hyper_data, n_row};
-    s = run_impl(h, a);
-    const std::string keep = g_err;
-    ggdmc_destroy(h);
-    g_err = keep;
-    return s;
+    return run_oneshot(nullptr, nullptr, a);
 }
 
 static RunDev loglik_desc(ggdmc_handle *h, int prec)

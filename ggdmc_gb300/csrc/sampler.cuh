@@ -33,6 +33,15 @@ enum StatIdx { ST_PROPOSALS = 0, ST_ACCEPTS, ST_MIGRATIONS, ST_REEVALS, ST_TRIAL
 constexpr int kVariants = 8;
 
 
+// Partial log-likelihood sums of one proposal over a range of a subject's
+// trials (group_chunk): the double-float sum of the FP32 mantissa logs,
+// their binary exponents, the trials left to FP64 and the FP64 terms.
+struct JobPart {
+    float h, l;
+    int32_t e, nf;
+    double f64;
+};
+
 struct RunDev {
     // ------------------------------------------------------------ shape
     int32_t C;            // chains

@@ -523,10 +523,14 @@ struct WarpPart {
     int e, nf;
 };
 constexpr int kWpDoubles = kGroup * 32 * (int)(sizeof(WarpPart) / sizeof(double));
-static_assert(kWpDoubles + 2 * kGroup <= kRedDoubles, "sm.red holds the warp partials and the results");
+static_assert(kWpDoubles + kGroup + kGroup * sizeof(JobPart) / sizeof(double) <= kRedDoubles,
+              "sm.red holds the warp partials, the results and the job parts");
 __device__ __forceinline__ WarpPart *warp_parts(const SubSmem &sm) { return reinterpret_cast<WarpPart *>(sm.red); }
 __device__ __forceinline__ double *group_res(const SubSmem &sm) { return sm.red + kWpDoubles; }
-__device__ __forceinline__ int *group_nf(const SubSmem &sm) { return reinterpret_cast<int *>(sm.red + kWpDoubles + kGroup); }
+__device__ __forceinline__ JobPart *job_parts(const SubSmem &sm)
+{
+    return reinterpret_cast<JobPart *>(sm.red + kWpDoubles + kGroup);
+}
 
 // Kahan-compensated FP32 accumulation (sum s, compensation c)
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
@@ -597,27 +601,28 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
 // kLba4 only the 4-accumulator LBA loop.
 constexpr int kAnyModel = 0, kLbaOnly = 1, kDdmOnly = 2, kLba4 = 3;
 
-// Log-likelihood sums of the subject's trials for the ng (<= kGroup)
-// proposals loaded in sm, on the whole CTA; out[g] valid on all threads.
-// MIXED: a trial's log density is log g_w (in FP64, once per cell through
-// the subject's cell counts) + e ln 2 + log m from lba_ld32; warp g combines
-// proposal g's warp partials and its per-cell constant.  FP64 tables are
-// built only for a proposal some trial of which needs the FP64 form, and
-// only those trials use it.
+// Partial log-likelihood sums of trials [i0, i1) of subject level l for the
+// ng (<= kGroup) proposals loaded in sm, on the whole CTA, into parts[g]
+// (shared memory; valid on all threads on return).  MIXED LBA: the FP32
+// pass (lba_group_loop32) leaves per-warp partials that warp g combines for
+// proposal g; a trial's log density is log g_w + e ln 2 + log m, and log g_w
+// is NOT included here (group_cell_const adds it once per cell).  FP64
+// tables are built only for a proposal some trial of which needs the FP64
+// form, and only those trials use it; their FP64 value, less log g_w, goes
+// to parts[g].f64.  FP64 and the diffusion model: parts[g].f64 only.
 template <int MODEL = kAnyModel>
-__device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool mixed, double *out)
+__device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed, JobPart *parts)
 {
-    const int64_t base = r.offs[l];
-    const int n = (int)(r.offs[l + 1] - base);
-    if constexpr (MODEL == kDdmOnly) {
-        ddm_group_loglik(r, l, 0, n, sm, ng, mixed, out);
+    const int64_t base = r.offs[l] + i0;
+    const int n = i1 - i0;
+    bool ddm = MODEL == kDdmOnly;
+    if constexpr (MODEL == kAnyModel) ddm = r.m.model_type == kModelDdm;
+    if (ddm) {
+        double o[kGroup];
+        ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, o);
+        if (threadIdx.x < ng) parts[threadIdx.x] = JobPart{0.f, 0.f, 0, 0, o[threadIdx.x]};
+        __syncthreads();
         return;
-    }
-    if constexpr (MODEL == kAnyModel) {
-        if (r.m.model_type == kModelDdm) {
-            ddm_group_loglik(r, l, 0, n, sm, ng, mixed, out);
-            return;
-        }
     }
     const int K = r.m.n_acc;
     const int NE = r.m.n_ent, NT = r.m.n_t0;
@@ -627,8 +632,10 @@ __device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool m
             __syncthreads();
             double acc = 0.0;
             for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
-            out[g] = block_sum(acc, sm.red);
+            const double tot = block_sum(acc, sm.red);
+            if (threadIdx.x == 0) parts[g] = JobPart{0.f, 0.f, 0, 0, tot};
         }
+        __syncthreads();
         return;
     }
     if (threadIdx.x == 0) *sm.fbn = 0;
@@ -642,26 +649,15 @@ __device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool m
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const WarpPart *wp = warp_parts(sm);
-    double *res = group_res(sm);
-    int *gnf = group_nf(sm);
-    const int32_t *cnt = r.cell_cnt + (size_t)l * r.m.n_cell;
     for (int g = wid; g < ng; g += nw) {
         float hh = 0.f, ll = 0.f;
         int ee = 0, nf = 0;
-        double dc = 0.0;
-        if (sm.flag[g] == 0) {
-            if (lane < nw) {
-                const WarpPart p = wp[g * 32 + lane];
-                hh = p.h;
-                ll = p.l;
-                ee = p.e;
-                nf = p.nf;
-            }
-            // log g of each trial's winning tuple, by cell: sum over cells of n_c log g
-            for (int c = lane; c < r.m.n_cell; c += 32) {
-                const int nc = cnt[c];
-                if (nc) dc += (double)nc * sm.lg[g * NE + sm.cent[c * K]];
-            }
+        if (sm.flag[g] == 0 && lane < nw) {
+            const WarpPart p = wp[g * 32 + lane];
+            hh = p.h;
+            ll = p.l;
+            ee = p.e;
+            nf = p.nf;
         }
         for (int o = 16; o > 0; o >>= 1) {
             const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
@@ -669,54 +665,93 @@ __device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool m
             ff_add(hh, ll, h2, l2);
             ee += __shfl_down_sync(0xffffffffu, ee, o);
             nf += __shfl_down_sync(0xffffffffu, nf, o);
-            dc += __shfl_down_sync(0xffffffffu, dc, o);
         }
-        if (lane == 0) {
-            res[g] = dc + ((double)hh + (double)ll) + kLn2 * (double)ee;
-            gnf[g] = nf;
-        }
+        if (lane == 0) parts[g] = JobPart{hh, ll, ee, nf, 0.0};
     }
     __syncthreads();
     bool anyfb = false;
-    for (int g = 0; g < ng; ++g) anyfb |= gnf[g] > 0 || sm.flag[g] != 0;
-    if (anyfb) {
-        // FP64 for the listed trials (their log g was counted above, so it is
-        // taken back out), or for every trial of a proposal outside the FP32
-        // form's domain
-        for (int g = 0; g < ng; ++g) {
-            const bool usable = sm.flag[g] == 0;
-            if (usable && gnf[g] == 0) continue;    // uniform over the block
-            build_tables64(r, sm, sm.theta + g * kMaxTheta);
-            if (r.stats && threadIdx.x == 0)
-                atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)(usable ? gnf[g] : n));
-            __syncthreads();
-            const int fbn = *sm.fbn;
-            double acc = 0.0;
-            if (!usable) {
-                for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
-            } else if (fbn <= kFbCap) {
-                for (int q = threadIdx.x; q < fbn; q += blockDim.x) {
-                    const int e = sm.fb[q];
-                    if ((e & 3) != g) continue;
-                    const int i = e >> 2, c = r.cell[base + i];
-                    acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
-                }
-            } else {
-                for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                    const int c = r.cell[base + i];
-                    int ex;
-                    float lm;
-                    if (lba_ld32_n(r.rt32[base + i], sm.t032[g * NT + sm.ct0[c]], sm.cent + c * K, K, sm.e32 + g * NE,
-                                   ex, lm))
-                        continue;
-                    acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
-                }
+    for (int g = 0; g < ng; ++g) anyfb |= parts[g].nf > 0 || sm.flag[g] != 0;
+    if (!anyfb) return;
+    // FP64 for the listed trials (log g_w taken back out: the cell constant
+    // counts it for every trial), or for every trial of a proposal outside
+    // the FP32 form's domain
+    for (int g = 0; g < ng; ++g) {
+        const bool usable = sm.flag[g] == 0;
+        const int nfg = parts[g].nf;
+        if (usable && nfg == 0) continue;           // uniform over the block
+        build_tables64(r, sm, sm.theta + g * kMaxTheta);
+        if (r.stats && threadIdx.x == 0)
+            atomicAdd(&r.stats[ST_FALLBACKS], (unsigned long long)(usable ? nfg : n));
+        __syncthreads();
+        const int fbn = *sm.fbn;
+        double acc = 0.0;
+        if (!usable) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
+        } else if (fbn <= kFbCap) {
+            for (int q = threadIdx.x; q < fbn; q += blockDim.x) {
+                const int e = sm.fb[q];
+                if ((e & 3) != g) continue;
+                const int i = e >> 2, c = r.cell[base + i];
+                acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
             }
-            const double tot = block_sum(acc, sm.red);      // red[0..32]: the warp partials are consumed
-            if (threadIdx.x == 0) res[g] += tot;
-            __syncthreads();
+        } else {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int c = r.cell[base + i];
+                int ex;
+                float lm;
+                if (lba_ld32_n(r.rt32[base + i], sm.t032[g * NT + sm.ct0[c]], sm.cent + c * K, K, sm.e32 + g * NE,
+                               ex, lm))
+                    continue;
+                acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
+            }
         }
+        const double tot = block_sum(acc, sm.red);  // red[0..32]: the warp partials are consumed
+        if (threadIdx.x == 0) parts[g].f64 += tot;
+        __syncthreads();
     }
+}
+
+// The per-cell FP64 constant of a MIXED LBA proposal, on one warp (every
+// lane gets it): sum over cells of n_c log g_w (lg [n_ent], the proposal's
+// log g of each tuple).
+__device__ __forceinline__ double group_cell_const(const RunDev &r, int l, const double *lg, const uint8_t *cent)
+{
+    const int lane = threadIdx.x & 31, K = r.m.n_acc;
+    const int32_t *cnt = r.cell_cnt + (size_t)l * r.m.n_cell;
+    double dc = 0.0;
+    for (int c = lane; c < r.m.n_cell; c += 32) {
+        const int nc = cnt[c];
+        if (nc) dc += (double)nc * lg[cent[c * K]];
+    }
+    for (int o = 16; o > 0; o >>= 1) dc += __shfl_down_sync(0xffffffffu, dc, o);
+    return __shfl_sync(0xffffffffu, dc, 0);
+}
+
+// The sum of a proposal from its parts and its cell constant (dc = 0 where
+// the FP32 form was not used).
+__device__ __forceinline__ double part_total(const JobPart &p, double dc)
+{
+    return dc + ((double)p.h + (double)p.l) + kLn2 * (double)p.e + p.f64;
+}
+
+// Log-likelihood sums of the subject's trials for the ng (<= kGroup)
+// proposals loaded in sm, on the whole CTA; out[g] valid on all threads.
+template <int MODEL = kAnyModel>
+__device__ void group_loglik(const RunDev &r, int l, SubSmem &sm, int ng, bool mixed, double *out)
+{
+    const int n = (int)(r.offs[l + 1] - r.offs[l]);
+    JobPart *parts = job_parts(sm);
+    double *res = group_res(sm);
+    group_chunk<MODEL>(r, l, 0, n, sm, ng, mixed, parts);
+    bool lba = MODEL != kDdmOnly;
+    if constexpr (MODEL == kAnyModel) lba = r.m.model_type != kModelDdm;
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int g = wid; g < ng; g += nw) {
+        const double dc = (mixed && lba && sm.flag[g] == 0)
+                              ? group_cell_const(r, l, sm.lg + g * r.m.n_ent, sm.cent) : 0.0;
+        if ((threadIdx.x & 31) == 0) res[g] = part_total(parts[g], dc);
+    }
+    __syncthreads();
     for (int g = 0; g < ng; ++g) out[g] = res[g];
     __syncthreads();
 }

@@ -115,7 +115,7 @@ def _draw_ptr(m, draws):
 
 
 def stats_dict(st: abi.RunStats) -> dict:
-    return {k: (float(getattr(st, k)) if k == "sweep_ms" else int(getattr(st, k)))
+    return {k: (float(getattr(st, k)) if k.endswith("_ms") else int(getattr(st, k)))
             for k, _ in abi.RunStats._fields_}
 
 

@@ -143,6 +143,11 @@ typedef struct {
     int64_t resolve_rounds;    /* ordered-decision rounds over all subject passes */
     int64_t variants;          /* migration steps evaluated ahead of their decision */
     int64_t fallbacks;         /* MIXED: trial densities re-evaluated in FP64 */
+    /* host wall-clock of the call's phases, ms */
+    double setup_ms;           /* handle creation and uploads (one-shot calls), run buffers, start state */
+    double capture_ms;         /* CUDA graph capture and instantiation (or reuse of the handle's graph) */
+    double run_ms;             /* graph replays, with the sample copies that overlap them */
+    double copyout_ms;         /* final state, remaining samples, counters; handle release (one-shot) */
 } ggdmc_run_stats;
 
 typedef struct ggdmc_handle ggdmc_handle;
