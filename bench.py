@@ -309,6 +309,15 @@ def run_ours(args):
     phi, subj = start_state(w, gpu, h)
     peak_fp32, peak_mufu = gpu.probe_peaks()
 
+    # the autotuner's settings for this design and data shape (cached in the
+    # process; one-shot ggdmc_run calls of the same shape use them too)
+    tuning = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tuning = h.autotune(cfg_for(w, args.warmup, abi.MIXED, abi.FLAG_L2_FLUSH), w.p_prior, *subj,
+                            h_table=w.h_prior, phi=phi, n_probe=4)
+        tune_s = time.perf_counter() - t0
+
     # warm-up (also compiles nothing: the library is prebuilt)
     wu = cfg_for(w, args.warmup, abi.MIXED, abi.FLAG_L2_FLUSH)
     h.run(wu, w.p_prior, *subj, h_table=w.h_prior, phi=phi)   # (phi None: independent fits)
@@ -323,6 +332,14 @@ def run_ours(args):
         wall = time.perf_counter() - t0
     st = out["stats"]
     ms = st["sweep_ms"]
+    tune_line = None
+    if tuning is not None:
+        # the same timed run under the built-in settings, for comparison
+        h.set_tuning(None)
+        dflt = h.run(cfg, w.p_prior, *subj, h_table=w.h_prior, phi=phi)["stats"]["sweep_ms"]
+        h.set_tuning({k: v for k, v in tuning.items()})
+        tune_line = dict(tuning, ms_per_step_tuned=round(ms / args.steps, 4),
+                         ms_per_step_default=round(dflt / args.steps, 4), tune_s=round(tune_s, 2))
     if args.profile:
         lk_ms, lk_evals = loglik_roofline(w, h, n_launch=2)
         log(f"profile mode: {args.steps} sweeps in {ms:.3f} ms; likelihood launch {lk_ms:.3f} ms")
@@ -351,6 +368,7 @@ def run_ours(args):
                 "fp64_fallback_fraction": round(st["fallbacks"] / max(st["trial_evals"], 1), 6),
                 "fp64_batched_sweeps_per_s": round(fp64_sweeps_s, 3),
                 "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
+                "tuning": tune_line,
                 "clocks": clk.summary()}
         line["config"] = config_of(w, world)
         if not args.no_cpu:
@@ -406,6 +424,7 @@ def run_ours(args):
         "reevaluations_per_sweep": round(st["reevaluations"] / args.steps, 2),
         "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
         "gpu_launches": int(st["kernel_launches"]),
+        "tuning": tune_line,
         "roofline": {"kernel": "loglik (k_loglik_batch = k_sub_loglik body)",
                      "bound": "fp32", "achieved": round(ach_tflops, 3),
                      "peak": round(peak_fp32, 3), "unit": "TFLOP/s",
@@ -427,7 +446,17 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(h2d // e2e_steps), "d2h_bytes_per_step": int(d2h // e2e_steps),
                 "steps": e2e_steps,
                 "call": "ggdmc_run (one-shot C ABI: upload, sweeps, sample download; "
-                        "one untimed call first)"},
+                        "one untimed call first)",
+                # host wall-clock of the call's phases (ggdmc_run_stats) and the
+                # Python marshalling around it
+                "breakdown_ms": {"total": round(e2e_s * 1e3, 3),
+                                 "create_upload": round(e2e["stats"]["setup_ms"], 3),
+                                 "graph_capture": round(e2e["stats"]["capture_ms"], 3),
+                                 "sweeps_and_sample_copies": round(e2e["stats"]["run_ms"], 3),
+                                 "copy_out_release": round(e2e["stats"]["copyout_ms"], 3),
+                                 "python": round(e2e_s * 1e3 - sum(e2e["stats"][k] for k in (
+                                     "setup_ms", "capture_ms", "run_ms", "copyout_ms")), 3),
+                                 "device_sweeps": round(e2e["stats"]["sweep_ms"], 3)}},
         "clocks": clk.summary(),
         "wall_s_timed_run": round(wall, 3),
     }
@@ -481,6 +510,7 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS),
                     help="another configuration, reported in a reduced line (default: the "
                          "256-subject uneven workload of the contract line)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch settings)")
     ap.add_argument("--profile", action="store_true",
                     help="warm-up and timed sweeps only (for ncu launch lists and captures)")
     args = ap.parse_args()

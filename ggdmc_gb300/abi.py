@@ -66,6 +66,14 @@ class Diag(C.Structure):
 PSRF_REFERENCE, PSRF_CODA = 0, 1
 
 
+class Tuning(C.Structure):
+    _fields_ = [("spec_group", C.c_int32), ("graph_iters", C.c_int32), ("mig_round", C.c_int32),
+                ("lik_variant", C.c_int32), ("sweep_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RunStats(C.Structure):
     _fields_ = [("proposals", C.c_int64), ("accepts", C.c_int64), ("migrations", C.c_int64),
                 ("reevaluations", C.c_int64), ("kernel_launches", C.c_int64),
@@ -126,11 +134,7 @@ class Marshal:
         theta = self.keep(np.array(theta, dtype=np.float64, order="C", copy=True))
         lp = self.keep(np.array(lp, dtype=np.float64, order="C", copy=True))
         ll = self.keep(np.array(ll, dtype=np.float64, order="C", copy=True))
-        n = theta.shape[0]
-        arr = (ChainState * n)()
-        for i in range(n):
-            arr[i] = ChainState(dptr(theta[i]), dptr(lp[i]), dptr(ll[i]))
-        self.keep(arr)
+        arr = self.ptr_table(ChainState, theta, lp, ll)
         return arr, theta, lp, ll
 
     def samples(self, n_level, nmc, nchain, npar):
@@ -139,11 +143,19 @@ class Marshal:
         theta = self.keep(np.empty((n_level, nmc, nchain, npar)))
         lp = self.keep(np.empty((n_level, nmc, nchain)))
         ll = self.keep(np.empty((n_level, nmc, nchain)))
-        arr = (Samples * n_level)()
-        for i in range(n_level):
-            arr[i] = Samples(dptr(theta[i]), dptr(lp[i]), dptr(ll[i]))
-        self.keep(arr)
+        arr = self.ptr_table(Samples, theta, lp, ll)
         return arr, theta, lp, ll
+
+    def ptr_table(self, struct, *arrs):
+        """An array of `struct` (all of whose fields are double pointers),
+        entry i pointing at arrs[k][i]; built in one numpy pass."""
+        n = arrs[0].shape[0]
+        tab = np.empty((n, len(arrs)), dtype=np.uintp)
+        idx = np.arange(n, dtype=np.uintp)
+        for k, a in enumerate(arrs):
+            tab[:, k] = np.uintp(a.ctypes.data) + idx * np.uintp(a.strides[0])
+        self.keep(tab)
+        return (struct * n).from_buffer(tab)
 
 
 @dataclass

@@ -6,6 +6,7 @@
 // graph and replays it, then copies the thinned samples back into the
 // caller's arrays (R's posterior layout).
 #include <algorithm>
+#include <utility>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -13,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -194,6 +196,7 @@ struct ggdmc_handle {
     DevBuf<double> ref_partial;
     DevBuf<uint8_t> flushbuf;
     PinnedBuf stage[2];                   // sample chunks on their way to the caller's buffers
+    ggdmc_tuning tuning{};                // launch settings (0: built-in choice)
 
     DevModel dev_model() const
     {
@@ -421,13 +424,25 @@ ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
     // density).  A subject's sums do not depend on the order beyond
     // rounding; perm maps a stored trial back to its place in the data.
     std::vector<int64_t> perm(N);
+    std::vector<int64_t> pos(h->n_cell);
+    std::vector<std::pair<double, int64_t>> seg;
     for (int s = 0; s < S; ++s) {
-        int64_t *b = perm.data() + offs[s], *e = perm.data() + offs[s + 1];
-        std::iota(b, e, offs[s]);
-        std::stable_sort(b, e, [&](int64_t x, int64_t y) {
-            return d->cell[x] != d->cell[y] ? d->cell[x] < d->cell[y] : d->rt[x] < d->rt[y];
-        });
-        for (int64_t *q = b; q < e; ++q) ++cnt[(size_t)s * h->n_cell + d->cell[*q]];
+        int32_t *cs = cnt.data() + (size_t)s * h->n_cell;
+        for (int64_t i = offs[s]; i < offs[s + 1]; ++i) ++cs[d->cell[i]];
+        int64_t at = offs[s];
+        for (int c = 0; c < h->n_cell; ++c) {
+            pos[c] = at;
+            at += cs[c];
+        }
+        for (int64_t i = offs[s]; i < offs[s + 1]; ++i) perm[pos[d->cell[i]]++] = i;   // by cell, stable
+        for (int c = 0, b = 0; c < h->n_cell; b += cs[c], ++c) {
+            if (cs[c] < 2) continue;
+            int64_t *q = perm.data() + offs[s] + b;
+            seg.resize(cs[c]);
+            for (int j = 0; j < cs[c]; ++j) seg[j] = {d->rt[q[j]], q[j]};
+            std::sort(seg.begin(), seg.end());     // by RT, then data order
+            for (int j = 0; j < cs[c]; ++j) q[j] = seg[j].second;
+        }
     }
     std::vector<double> r64(N);
     std::vector<float2> r32(N);
@@ -547,6 +562,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     // 0.595 at 4), the diffusion model and the 2-accumulator fits at 1
     // (hier_ddm_64 2.34 / 2.43 / 3.10 ms, many_fits_1024 3.44 / 3.75 / 4.56 ms).
     int spec_group = (h->model_type == GGDMC_MODEL_DDM || h->n_acc < 4) ? 1 : 2;
+    if (h->tuning.spec_group > 0) spec_group = std::min(4, h->tuning.spec_group);
     if (const char *gs = std::getenv("GGDMC_SPEC_GROUP")) spec_group = std::min(4, std::max(1, std::atoi(gs)));
     int n_spec_items = 0;
     if (S > 0) {
@@ -714,6 +730,12 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.spec_cnt = fused ? h->spec_cnt.p : nullptr;
     r.ctl = fused ? h->ctl.p : nullptr;
     r.iter_end = (int32_t)n_iter;
+    // migration steps evaluated ahead per resolve round: 4 measured 4% faster
+    // than 8 and 2% faster than 3 on the 256-subject workload
+    r.mig_round = h->tuning.mig_round > 0 ? h->tuning.mig_round : 4;
+    if (const char *mr = std::getenv("GGDMC_MIG_ROUND")) r.mig_round = std::max(1, std::atoi(mr));
+    r.lik_variant = h->tuning.lik_variant == 2 ? 1 : 0;
+    if (const char *lv = std::getenv("GGDMC_LIK_VARIANT")) r.lik_variant = std::atoi(lv) == 2 ? 1 : 0;
     // GGDMC_SPEC_IDLE_LIMIT: polls before an idle CTA of the fused schedule
     // gives up waiting (default 2^21, about 2 s); the run then completes and
     // returns GGDMC_ERR_TIMEOUT
@@ -808,7 +830,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     const bool flush = (c.flags & GGDMC_FLAG_L2_FLUSH) != 0;
     if (n_iter > 0) {
         const char *gs = std::getenv("GGDMC_GRAPH_ITERS");
-        int64_t per_graph = gs ? std::max(1, std::atoi(gs)) : 8;
+        int64_t per_graph = h->tuning.graph_iters > 0 ? std::min(64, h->tuning.graph_iters) : 8;
+        if (gs) per_graph = std::max(1, std::atoi(gs));
         per_graph = std::min<int64_t>(per_graph, n_iter);
         if (flush) CU(h->flushbuf.alloc(kFlushBytes));
         std::vector<cudaEvent_t> ev_a(per_graph + 1), ev_b(per_graph + 1);
@@ -818,32 +841,43 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             for (auto &e : ev_a) cudaEventDestroy(e);
             for (auto &e : ev_b) cudaEventDestroy(e);
         };
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
+        // two graphs: per_graph iterations, replayed while at least that many
+        // remain, and the remainder (n_iter % per_graph), so that every
+        // iteration runs from a graph and its samples leave by the pipeline
+        cudaGraph_t graph = nullptr, graph_tail = nullptr;
+        cudaGraphExec_t exec = nullptr, exec_tail = nullptr;
         t_setup = ms_since(t_in);
         const auto t_cap = std::chrono::steady_clock::now();
-        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        cudaError_t ce = cudaSuccess;
-        launches_per_iter = 0;
-        for (int64_t i = 0; i < per_graph && ce == cudaSuccess; ++i) {
-            // external event nodes: recorded (and timeable) on every replay
-            if (flush) ce = cudaEventRecordWithFlags(ev_a[i], st, cudaEventRecordExternal);
-            if (!ce) ce = one_iteration();
-            if (flush && !ce) ce = cudaEventRecordWithFlags(ev_b[i], st, cudaEventRecordExternal);
-            if (flush && !ce) ce = cudaMemsetAsync(h->flushbuf.p, (int)(i & 0xff), kFlushBytes, st);
-        }
-        cudaError_t ee = cudaStreamEndCapture(st, &graph);
-        if (ce || ee) {
-            cleanup_events();
+        const int64_t rem = n_iter % per_graph;
+        auto capture = [&](int64_t iters, cudaGraph_t &g, cudaGraphExec_t &x) -> ggdmc_status {
+            CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            cudaError_t ce = cudaSuccess;
+            launches_per_iter = 0;
+            for (int64_t i = 0; i < iters && ce == cudaSuccess; ++i) {
+                // external event nodes: recorded (and timeable) on every replay
+                if (flush) ce = cudaEventRecordWithFlags(ev_a[i], st, cudaEventRecordExternal);
+                if (!ce) ce = one_iteration();
+                if (flush && !ce) ce = cudaEventRecordWithFlags(ev_b[i], st, cudaEventRecordExternal);
+                if (flush && !ce) ce = cudaMemsetAsync(h->flushbuf.p, (int)(i & 0xff), kFlushBytes, st);
+            }
+            cudaError_t ee = cudaStreamEndCapture(st, &g);
+            if (ce || ee) return fail(GGDMC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce ? ce : ee));
+            cudaError_t ie = cudaGraphInstantiateWithFlags(&x, g, cudaGraphInstantiateFlagUseNodePriority);
+            if (ie) return fail(GGDMC_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+            return GGDMC_OK;
+        };
+        auto destroy_graphs = [&]() {
+            if (exec) cudaGraphExecDestroy(exec);
             if (graph) cudaGraphDestroy(graph);
-            return fail(GGDMC_ERR_CUDA, std::string("graph capture: ") +
-                                            cudaGetErrorString(ce ? ce : ee));
-        }
-        cudaError_t ie = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
-        if (ie) {
+            if (exec_tail) cudaGraphExecDestroy(exec_tail);
+            if (graph_tail) cudaGraphDestroy(graph_tail);
+        };
+        ggdmc_status cs_ = rem ? capture(rem, graph_tail, exec_tail) : GGDMC_OK;
+        if (!cs_) cs_ = capture(per_graph, graph, exec);
+        if (cs_) {
             cleanup_events();
-            cudaGraphDestroy(graph);
-            return fail(GGDMC_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+            destroy_graphs();
+            return cs_;
         }
         const int64_t per_iter = launches_per_iter / per_graph;
         int64_t done = 0;
@@ -880,8 +914,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             if (pe) {
                 destroy_pipe();
                 cleanup_events();
-                cudaGraphExecDestroy(exec);
-                cudaGraphDestroy(graph);
+                destroy_graphs();
                 return fail(GGDMC_ERR_CUDA, std::string("sample staging: ") + cudaGetErrorString(pe));
             }
         }
@@ -942,13 +975,15 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         t_capture = ms_since(t_cap);
         const auto t_rep = std::chrono::steady_clock::now();
         if (!flush) CU(cudaEventRecord(ev_a[per_graph], st));
-        while (done + per_graph <= n_iter && !ws) {
-            cudaError_t e = cudaGraphLaunch(exec, st);
+        while (done < n_iter && !ws) {
+            const bool full = done + per_graph <= n_iter;
+            const int64_t iters = full ? per_graph : rem;
+            cudaError_t e = cudaGraphLaunch(full ? exec : exec_tail, st);
             if (e) {
                 ws = fail(GGDMC_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
                 break;
             }
-            done += per_graph;
+            done += iters;
             if (pipe) {
                 const int b = (int)(rep & 1);
                 e = cudaEventRecord(ev_rep[b], st);
@@ -967,7 +1002,7 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             // read this replay's event nodes before the next replay reuses them
             ws = wait_stream(st);
             if (ws) break;
-            for (int64_t i = 0; i < per_graph && !ws; ++i) {
+            for (int64_t i = 0; i < iters && !ws; ++i) {
                 float ms = 0.f;
                 cudaError_t te = cudaEventElapsedTime(&ms, ev_a[i], ev_b[i]);
                 if (te) ws = fail(GGDMC_ERR_CUDA, std::string("cudaEventElapsedTime: ") +
@@ -983,25 +1018,9 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             sweep_ms += ms;
         }
         if (pipe && rep >= 1 && !ws) ws = drain((int)((rep - 1) & 1));
-        for (; done < n_iter && !ws; ++done) {
-            launches_per_iter = 0;
-            cudaError_t e = cudaEventRecord(ev_a[per_graph], st);
-            if (!e) e = one_iteration();
-            if (!e) e = cudaEventRecord(ev_b[per_graph], st);
-            if (e) {
-                ws = fail(GGDMC_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
-                break;
-            }
-            ws = wait_stream(st);
-            float ms = 0.f;
-            if (!ws) cudaEventElapsedTime(&ms, ev_a[per_graph], ev_b[per_graph]);
-            sweep_ms += ms;
-            if (flush && !ws) cudaMemsetAsync(h->flushbuf.p, 0, kFlushBytes, st);
-        }
         launches += n_iter * per_iter;
         t_run = ms_since(t_rep);
-        cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(graph);
+        destroy_graphs();
         cleanup_events();
         destroy_pipe();
         if (ws) return ws;
@@ -1233,6 +1252,15 @@ static ggdmc_status run_oneshot(const ggdmc_model *model, const ggdmc_data *data
     ggdmc_status s = make_handle(model, data, &h);
     if (s) return s;
     const double t_make = ms_since(t0);
+    // settings the autotuner found for this shape earlier in the process
+    if (model && data && a.cfg) {
+        char key[512];
+        ggdmc_tuning t{};
+        if (!ggdmc_tune_key(model, data, a.cfg->nchain, a.kind == RK_HIER, key, sizeof key) &&
+            !ggdmc_tune_lookup(key, nullptr, &t))
+            h->tuning = t;
+        g_err.clear();
+    }
     s = run_impl(h, a);
     const std::string keep = g_err;
     const auto t1 = std::chrono::steady_clock::now();
@@ -1591,6 +1619,196 @@ ggdmc_status ggdmc_loghlike(const ggdmc_prior *p_prior, const double *phi, const
     cudaFree(d_out);
     if (e) return fail(GGDMC_ERR_CUDA, std::string("loghlike: ") + cudaGetErrorString(e));
     return GGDMC_OK;
+}
+
+// ------------------------------------------------------------ tuning
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::string, ggdmc_tuning> g_tune_cache;   // this process's autotuner cache
+
+int pow2_floor(int64_t x)
+{
+    int k = 0;
+    while (x > 1) {
+        x >>= 1;
+        ++k;
+    }
+    return k;
+}
+
+}  // namespace
+
+ggdmc_status ggdmc_tune_key(const ggdmc_model *model, const ggdmc_data *data, int32_t nchain, int32_t hierarchical,
+                            char *key, int32_t key_len)
+{
+    if (!model || !data || !key || key_len < 1 || !data->offsets || data->n_subject < 0)
+        return fail(GGDMC_ERR_ARG, "bad tune_key arguments");
+    // trial counts by power of two; each bin's subject count by power of two
+    std::map<int, int64_t> bins;
+    for (int s = 0; s < data->n_subject; ++s) ++bins[pow2_floor(data->offsets[s + 1] - data->offsets[s])];
+    std::string k = (model->model_type == GGDMC_MODEL_DDM ? "ddm" : "lba") + std::to_string(model->n_acc) + ".p" +
+                    std::to_string(model->n_par) + ".c" + std::to_string(nchain) + (hierarchical ? ".h" : ".f") +
+                    ".s" + std::to_string(pow2_floor(std::max(data->n_subject, 1)));
+    for (const auto &b : bins) k += "." + std::to_string(b.first) + "x" + std::to_string(pow2_floor(b.second));
+    if ((int32_t)k.size() + 1 > key_len) return fail(GGDMC_ERR_ARG, "key buffer too small");
+    std::memcpy(key, k.c_str(), k.size() + 1);
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_tune_lookup(const char *key, const char *cache_path, ggdmc_tuning *out)
+{
+    if (!key || !out) return fail(GGDMC_ERR_ARG, "bad tune_lookup arguments");
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            *out = it->second;
+            return GGDMC_OK;
+        }
+    }
+    if (cache_path) {
+        if (FILE *f = std::fopen(cache_path, "r")) {
+            char kb[512];
+            ggdmc_tuning t{}, found{};
+            bool hit = false;
+            while (std::fscanf(f, "%511s %d %d %d %d %lf", kb, &t.spec_group, &t.graph_iters, &t.mig_round,
+                               &t.lik_variant, &t.sweep_ms) == 6)
+                if (std::strcmp(kb, key) == 0) {
+                    found = t;
+                    hit = true;
+                }
+            std::fclose(f);
+            if (hit) {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                g_tune_cache[key] = found;
+                *out = found;
+                return GGDMC_OK;
+            }
+        }
+    }
+    return fail(GGDMC_ERR_ARG, "no tuning cached for this key");
+}
+
+ggdmc_status ggdmc_tune_store(const char *key, const char *cache_path, const ggdmc_tuning *t)
+{
+    if (!key || !t || !*key || std::strchr(key, ' ') || std::strchr(key, '\n'))
+        return fail(GGDMC_ERR_ARG, "bad tune_store arguments");
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = *t;
+    }
+    if (cache_path) {
+        FILE *f = std::fopen(cache_path, "a");
+        if (!f) return fail(GGDMC_ERR_ARG, std::string("cannot append to ") + cache_path);
+        std::fprintf(f, "%s %d %d %d %d %.6f\n", key, t->spec_group, t->graph_iters, t->mig_round, t->lik_variant,
+                     t->sweep_ms);
+        std::fclose(f);
+    }
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_handle_set_tuning(ggdmc_handle *h, const ggdmc_tuning *t)
+{
+    if (!h) return fail(GGDMC_ERR_ARG, "handle is NULL");
+    h->tuning = t ? *t : ggdmc_tuning{};
+    return GGDMC_OK;
+}
+
+ggdmc_status ggdmc_autotune(ggdmc_handle *h, const ggdmc_de_config *cfg, const ggdmc_prior *p_prior,
+                            const ggdmc_prior *h_prior, const ggdmc_chain_state *phi_state,
+                            const ggdmc_chain_state *subj_state, int32_t n_probe, const char *cache_path,
+                            ggdmc_tuning *out)
+{
+    if (!h || !cfg || !p_prior || !subj_state || n_probe < 1) return fail(GGDMC_ERR_ARG, "bad autotune arguments");
+    if (h->S < 1) return fail(GGDMC_ERR_ARG, "handle has no subjects");
+    ggdmc_status s;
+    if ((s = check_cfg(cfg))) return s;
+    // the key from the handle's own design and trial counts
+    ggdmc_model m{};
+    m.model_type = h->model_type;
+    m.n_par = h->n_par;
+    m.n_acc = h->n_acc;
+    ggdmc_data d{};
+    d.n_subject = h->S;
+    d.offsets = h->h_offs.data();
+    char key[512];
+    if ((s = ggdmc_tune_key(&m, &d, cfg->nchain, phi_state != nullptr, key, sizeof key))) return s;
+    ggdmc_tuning best{};
+    if (!ggdmc_tune_lookup(key, cache_path, &best)) {
+        h->tuning = best;
+        if (out) *out = best;
+        return GGDMC_OK;
+    }
+    g_err.clear();
+    // probes: private copies of the start states, no samples kept
+    const int S = h->S, C = cfg->nchain, P = h->n_par;
+    std::vector<double> th((size_t)S * C * P), lp((size_t)S * C), ll((size_t)S * C);
+    std::vector<double> pth(phi_state ? (size_t)C * 2 * P : 0), plp(phi_state ? C : 0), pll(phi_state ? C : 0);
+    std::vector<ggdmc_chain_state> ss(S);
+    ggdmc_chain_state ps{};
+    ggdmc_de_config pc = *cfg;
+    pc.nmc = n_probe + 1;
+    pc.thin = 1;
+    auto probe = [&](const ggdmc_tuning &t, double &ms) -> ggdmc_status {
+        for (int l = 0; l < S; ++l) {
+            std::memcpy(th.data() + (size_t)l * C * P, subj_state[l].theta, sizeof(double) * C * P);
+            std::memcpy(lp.data() + (size_t)l * C, subj_state[l].lp, sizeof(double) * C);
+            std::memcpy(ll.data() + (size_t)l * C, subj_state[l].ll, sizeof(double) * C);
+            ss[l] = ggdmc_chain_state{th.data() + (size_t)l * C * P, lp.data() + (size_t)l * C, ll.data() + (size_t)l * C};
+        }
+        if (phi_state) {
+            std::memcpy(pth.data(), phi_state->theta, sizeof(double) * pth.size());
+            std::memcpy(plp.data(), phi_state->lp, sizeof(double) * C);
+            std::memcpy(pll.data(), phi_state->ll, sizeof(double) * C);
+            ps = ggdmc_chain_state{pth.data(), plp.data(), pll.data()};
+        }
+        h->tuning = t;
+        ggdmc_run_stats st{};
+        RunArgs a{phi_state ? RK_HIER : RK_SUBJECTS, &pc, p_prior, h_prior, phi_state ? &ps : nullptr, ss.data(),
+                  nullptr, nullptr, nullptr, &st, nullptr, 0};
+        ggdmc_status rs = run_impl(h, a);
+        ms = st.sweep_ms / std::max<int64_t>(1, st.iterations);
+        return rs;
+    };
+    // one setting at a time from the built-in choice; each probe runs twice
+    // (the first warms the graph and caches) and the second time counts
+    ggdmc_tuning cur{};
+    double cur_ms = 0.0;
+    auto measure = [&](const ggdmc_tuning &t, double &ms) -> ggdmc_status {
+        double w = 0.0;
+        ggdmc_status rs = probe(t, w);
+        if (!rs) rs = probe(t, ms);
+        return rs;
+    };
+    if ((s = measure(cur, cur_ms))) { h->tuning = ggdmc_tuning{}; return s; }
+    auto consider = [&](ggdmc_tuning t) -> ggdmc_status {
+        double ms = 0.0;
+        ggdmc_status rs = measure(t, ms);
+        if (rs) return rs;
+        if (ms < cur_ms * 0.99) {
+            cur = t;
+            cur_ms = ms;
+        }
+        return GGDMC_OK;
+    };
+    auto tweak = [&](int32_t ggdmc_tuning::*f, int32_t v) -> ggdmc_status {
+        ggdmc_tuning t = cur;
+        t.*f = v;
+        return consider(t);
+    };
+    if (h->model_type != GGDMC_MODEL_DDM && h->n_acc == 4) s = tweak(&ggdmc_tuning::lik_variant, 2);
+    for (int g : {1, 2, 4}) if (!s) s = tweak(&ggdmc_tuning::spec_group, g);
+    for (int mr : {3, 6, 8}) if (!s) s = tweak(&ggdmc_tuning::mig_round, mr);
+    for (int gi : {4, 16}) if (!s) s = tweak(&ggdmc_tuning::graph_iters, gi);
+    if (s) {
+        h->tuning = ggdmc_tuning{};
+        return s;
+    }
+    cur.sweep_ms = cur_ms;
+    h->tuning = cur;
+    if (out) *out = cur;
+    return ggdmc_tune_store(key, cache_path, &cur);
 }
 
 }  // extern "C"

@@ -116,6 +116,13 @@ struct RunDev {
     int32_t iter_end;              // last iteration of the run
     int32_t spec_idle_limit;       // polls (~1 us each) an idle k_sub_step CTA waits before giving up
 
+    // launch settings (ggdmc_tuning): migration variants evaluated per
+    // resolve round (1..kVariants), and the likelihood kernel of 4-accumulator
+    // LBA designs (0: the 4-accumulator instantiation at 8 CTAs per SM, 1: the
+    // generic one at 6); neither changes a result
+    int32_t mig_round;
+    int32_t lik_variant;
+
     unsigned long long *stats;     // [ST_N]
     int32_t *status;
 };

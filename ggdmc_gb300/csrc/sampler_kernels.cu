@@ -51,16 +51,10 @@ namespace ggdmc {
 
 constexpr int kLikThreads = 128;
 constexpr int kResolveThreads = GGDMC_RESOLVE_THREADS;
-// migration variants evaluated per resolve round (<= kVariants): 4 measured
-// 4% faster than 8 and 2% faster than 3 on the 256-subject workload
 // resolve migration levels first (1) or by trial count alone (0)
 #ifndef GGDMC_MIG_FIRST
 #define GGDMC_MIG_FIRST 1
 #endif
-#ifndef GGDMC_MIG_ROUND
-#define GGDMC_MIG_ROUND 4
-#endif
-constexpr int kMigRound = GGDMC_MIG_ROUND;
 constexpr int kPhiThreads = 256;
 constexpr int kProposeThreads = 512;
 // k_sub_step's claim counters (RunDev::ctl)
@@ -1331,6 +1325,8 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
         jit = js;
     }
     const int ct = threadIdx.x, cstride = blockDim.x;
+    // variants live in slots C + w, so at most C of them (CS = 2C)
+    const int mig_round = min(max(r.mig_round, 1), min(kVariants, C));
     int rounds = 0, reevals = 0, variants = 0;
     int decided = 0;
     if (type == PASS_CROSS) {
@@ -1437,7 +1433,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
             // source moved.  The value step s needs is fixed by the last
             // rejected step r before it: the spec proposal of step r+1 plus
             // the jitters of steps r+2..s, or, with no reject since d, the
-            // new source plus the jitters of d..s.  Evaluate the kMigRound
+            // new source plus the jitters of d..s.  Evaluate the r.mig_round
             // most likely of these, scored with this pass's acceptance so far.
             if (d > 0) {
                 if (threadIdx.x < 32) {
@@ -1445,7 +1441,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                     // (score a^c, 2 for c = 0); c >= kVariants: the value for
                     // step rj + 1 + k after a reject at rj = d + (c - kVariants) / 3,
                     // k = 1 + (c - kVariants) % 3 (score (1 - a) a^k 0.95^(rj - d));
-                    // the kMigRound best, ties to the lower c
+                    // the mig_round best, ties to the lower c
                     const int c = threadIdx.x;
                     const double a = (rs.misc[5] + 1.0) / (d + 2.0);
                     double sc = -1.0;
@@ -1475,12 +1471,12 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                         rank += (so > sc || (so == sc && o < c)) ? 1 : 0;
                     }
                     const bool valid = sc > 0.0;
-                    if (valid && rank < kMigRound) {
+                    if (valid && rank < mig_round) {
                         rs.vr[rank] = vr;
                         rs.vs[rank] = vs;
                     }
                     const int nvalid = __popc(__ballot_sync(0xffffffffu, valid));
-                    if (c == 0) rs.misc[4] = min(kMigRound, nvalid);
+                    if (c == 0) rs.misc[4] = min(mig_round, nvalid);
                 }
                 __syncthreads();
                 const int nv = rs.misc[4];
@@ -2470,7 +2466,7 @@ cudaError_t launch_sub_spec_rest(const RunDev &r, int group, cudaStream_t st)
     const size_t smem = sub_smem_bytes(r.m);
     if (r.m.model_type == kModelDdm)
         k_sub_spec_rest<GGDMC_LIK_MINB, kDdmOnly><<<r.S * bpl, kLikThreads, smem, st>>>(r, group, bpl);
-    else if (r.m.n_acc == 4)
+    else if (r.m.n_acc == 4 && r.lik_variant == 0)
         k_sub_spec_rest<GGDMC_LIK_MINB_LBA, kLba4><<<r.S * bpl, kLikThreads, smem, st>>>(r, group, bpl);
     else
         k_sub_spec_rest<GGDMC_LIK_MINB, kLbaOnly><<<r.S * bpl, kLikThreads, smem, st>>>(r, group, bpl);
@@ -2505,7 +2501,7 @@ cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items
     const size_t smem = sub_smem_bytes(r.m);
     if (r.m.model_type == kModelDdm)
         k_sub_loglik<GGDMC_LIK_MINB, kDdmOnly><<<n_items, kLikThreads, smem, st>>>(r, items, group);
-    else if (r.m.n_acc == 4)
+    else if (r.m.n_acc == 4 && r.lik_variant == 0)
         k_sub_loglik<GGDMC_LIK_MINB_LBA, kLba4><<<n_items, kLikThreads, smem, st>>>(r, items, group);
     else
         k_sub_loglik<GGDMC_LIK_MINB, kLbaOnly><<<n_items, kLikThreads, smem, st>>>(r, items, group);

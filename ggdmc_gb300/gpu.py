@@ -85,6 +85,17 @@ def lib():
     L.ggdmc_rebuild_posterior.restype = St
     L.ggdmc_rebuild_posterior.argtypes = [P(abi.Samples), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                           P(abi.Samples)]
+    L.ggdmc_tune_key.restype = St
+    L.ggdmc_tune_key.argtypes = [P(abi.Model), P(abi.Data), C.c_int32, C.c_int32, C.c_char_p, C.c_int32]
+    L.ggdmc_tune_lookup.restype = St
+    L.ggdmc_tune_lookup.argtypes = [C.c_char_p, C.c_char_p, P(abi.Tuning)]
+    L.ggdmc_tune_store.restype = St
+    L.ggdmc_tune_store.argtypes = [C.c_char_p, C.c_char_p, P(abi.Tuning)]
+    L.ggdmc_handle_set_tuning.restype = St
+    L.ggdmc_handle_set_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
+    L.ggdmc_autotune.restype = St
+    L.ggdmc_autotune.argtypes = [C.c_void_p, P(abi.DEConfig), P(abi.Prior), P(abi.Prior), P(abi.ChainState),
+                                 P(abi.ChainState), C.c_int32, C.c_char_p, P(abi.Tuning)]
     L.ggdmc_probe_peaks.restype = St
     L.ggdmc_probe_peaks.argtypes = [P(C.c_double), P(C.c_double)]
     _lib = L
@@ -208,6 +219,25 @@ class Handle:
         if phi:
             outs["phi"] = {k: v[0] for k, v in outs["phi"].items()}
         return outs
+
+    def set_tuning(self, tuning=None):
+        """Launch settings for this handle's runs (dict of ggdmc_tuning fields,
+        0 = built-in choice; None clears them)."""
+        t = abi.Tuning(**(tuning or {})) if tuning is not None else None
+        check(lib().ggdmc_handle_set_tuning(self.h, C.byref(t) if t is not None else None))
+
+    def autotune(self, cfg, p_table, theta, lp, ll, h_table=None, phi=None, n_probe=5, cache_path=None):
+        """ggdmc_autotune: the cached or freshly timed settings for runs like
+        cfg from these start states (not changed); the handle keeps them."""
+        m = abi.Marshal()
+        cc, cp = cfg.to_c(), m.prior(p_table)
+        ch = m.prior(h_table) if h_table is not None else None
+        st, *_ = m.states(theta, lp, ll)
+        pst = m.states(phi[0][None], phi[1][None], phi[2][None])[0] if phi is not None else None
+        out = abi.Tuning()
+        check(lib().ggdmc_autotune(self.h, C.byref(cc), C.byref(cp), C.byref(ch) if ch is not None else None,
+                                   pst, st, n_probe, cache_path.encode() if cache_path else None, C.byref(out)))
+        return out.as_dict()
 
     def trial_logdens(self, theta, precision=abi.FP64):
         """theta [S][P] -> per-trial log densities [N]."""
@@ -341,3 +371,23 @@ def rebuild_posteriors(runs):
     several hierarchical runs (each a gpu.run result) merged per subject."""
     S = runs[0]["subj_s"][0].shape[0]
     return [rebuild_posterior([tuple(x[s] for x in r["subj_s"]) for r in runs]) for s in range(S)]
+
+
+def tune_key(model, batch, nchain, hierarchical):
+    """The autotuner's cache key of a design and data shape (ggdmc_tune_key); host only."""
+    m = abi.Marshal()
+    buf = C.create_string_buffer(512)
+    check(lib().ggdmc_tune_key(C.byref(m.model(model)), C.byref(m.data(batch)), nchain, int(hierarchical), buf, 512))
+    return buf.value.decode()
+
+
+def tune_lookup(key, cache_path=None):
+    """Cached settings of a key (process cache, then the file), or None."""
+    out = abi.Tuning()
+    st = lib().ggdmc_tune_lookup(key.encode(), cache_path.encode() if cache_path else None, C.byref(out))
+    return out.as_dict() if st == 0 else None
+
+
+def tune_store(key, tuning, cache_path=None):
+    t = abi.Tuning(**tuning)
+    check(lib().ggdmc_tune_store(key.encode(), cache_path.encode() if cache_path else None, C.byref(t)))

@@ -340,6 +340,55 @@ ggdmc_status ggdmc_handle_diagnostics(ggdmc_handle *h, int32_t start, int32_t en
                                       const double *probs, int32_t n_prob, double conf,
                                       int32_t psrf_form, ggdmc_diag *subj, ggdmc_diag *phi);
 
+/* ------------------------------------------------------------ tuning
+ * Launch settings of a handle's runs.  None of them changes a result: the
+ * chains of a run are the same bit for bit under every setting.  0 in a
+ * field means "the built-in choice"; the environment variables
+ * GGDMC_SPEC_GROUP, GGDMC_GRAPH_ITERS, GGDMC_MIG_ROUND and GGDMC_LIK_VARIANT
+ * override a handle's settings. */
+typedef struct {
+    int32_t spec_group;        /* proposals per speculative likelihood CTA: 1, 2 or 4        */
+    int32_t graph_iters;       /* DE iterations per captured CUDA graph, 1..64              */
+    int32_t mig_round;         /* migration steps evaluated ahead per resolve round, 1..8   */
+    int32_t lik_variant;       /* 4-accumulator LBA: 1 = the 4-accumulator likelihood kernel
+                                  (8 CTAs per SM), 2 = the generic one (6 CTAs per SM)      */
+    double sweep_ms;           /* device time per sweep measured for the choice (output)   */
+} ggdmc_tuning;
+
+/* The autotuner's cache key of a design and data shape: model type,
+ * accumulators, free parameters, chains, whether a phi level runs, and the
+ * histogram of the subjects' trial counts in powers of two (each bin's count
+ * rounded to a power of two, so that similar data sets share a key).
+ * Writes a NUL-terminated key of at most key_len bytes.  Host only. */
+ggdmc_status ggdmc_tune_key(const ggdmc_model *model, const ggdmc_data *data, int32_t nchain,
+                            int32_t hierarchical, char *key, int32_t key_len);
+
+/* The cached settings of a key: from this process's cache, else from the
+ * text file cache_path (NULL: none; one "key spec_group graph_iters mig_round
+ * lik_variant sweep_ms" line per entry, the last line of a key wins).
+ * GGDMC_ERR_ARG when the key is not cached.  Host only. */
+ggdmc_status ggdmc_tune_lookup(const char *key, const char *cache_path, ggdmc_tuning *out);
+
+/* Put settings in this process's cache and, with cache_path, append them to
+ * the file.  Host only. */
+ggdmc_status ggdmc_tune_store(const char *key, const char *cache_path, const ggdmc_tuning *t);
+
+/* Settings for the runs of a handle (NULL: the built-in choices). */
+ggdmc_status ggdmc_handle_set_tuning(ggdmc_handle *h, const ggdmc_tuning *t);
+
+/* Autotune a handle for runs like cfg (its chains, level layout and
+ * precision): look the key up (cache_path as ggdmc_tune_lookup) and, when it
+ * is not cached, time candidate settings on n_probe DE iterations each from
+ * the given start states (which are not changed) -- the likelihood kernel
+ * variant, the speculative group size, the migration steps per round and the
+ * iterations per graph, one setting at a time from the built-in choice, by
+ * CUDA events on the device -- and store the fastest.  The handle then runs
+ * with it; *out (nullable) receives it. */
+ggdmc_status ggdmc_autotune(ggdmc_handle *h, const ggdmc_de_config *cfg, const ggdmc_prior *p_prior,
+                            const ggdmc_prior *h_prior, const ggdmc_chain_state *phi_state,
+                            const ggdmc_chain_state *subj_state, int32_t n_probe,
+                            const char *cache_path, ggdmc_tuning *out);
+
 /* Run on a resident handle: level layout as ggdmc_run (phi_state == NULL
  * runs the subjects as independent fits, like ggdmc_run_subjects). */
 ggdmc_status ggdmc_handle_run(ggdmc_handle *h, const ggdmc_de_config *cfg,
