@@ -424,35 +424,44 @@ ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
     // density).  A subject's sums do not depend on the order beyond
     // rounding; perm maps a stored trial back to its place in the data.
     std::vector<int64_t> perm(N);
-    std::vector<int64_t> pos(h->n_cell);
-    std::vector<std::pair<double, int64_t>> seg;
-    for (int s = 0; s < S; ++s) {
-        int32_t *cs = cnt.data() + (size_t)s * h->n_cell;
-        for (int64_t i = offs[s]; i < offs[s + 1]; ++i) ++cs[d->cell[i]];
-        int64_t at = offs[s];
-        for (int c = 0; c < h->n_cell; ++c) {
-            pos[c] = at;
-            at += cs[c];
-        }
-        for (int64_t i = offs[s]; i < offs[s + 1]; ++i) perm[pos[d->cell[i]]++] = i;   // by cell, stable
-        for (int c = 0, b = 0; c < h->n_cell; b += cs[c], ++c) {
-            if (cs[c] < 2) continue;
-            int64_t *q = perm.data() + offs[s] + b;
-            seg.resize(cs[c]);
-            for (int j = 0; j < cs[c]; ++j) seg[j] = {d->rt[q[j]], q[j]};
-            std::sort(seg.begin(), seg.end());     // by RT, then data order
-            for (int j = 0; j < cs[c]; ++j) q[j] = seg[j].second;
-        }
-    }
     std::vector<double> r64(N);
-    std::vector<float2> r32(N);
     std::vector<uint16_t> c16(N);
-    for (int64_t j = 0; j < N; ++j) {
-        const double rt = d->rt[perm[j]];
-        const float hi = (float)rt;
-        r64[j] = rt;
-        r32[j] = make_float2(hi, (float)(rt - (double)hi));
-        c16[j] = (uint16_t)d->cell[perm[j]];
+    // subjects in blocks over host threads (each writes only its subjects'
+    // ranges of perm, cnt, r64 and c16)
+    auto sort_subjects = [&](int s0, int s1) {
+        std::vector<int64_t> pos(h->n_cell);
+        std::vector<std::pair<double, int64_t>> seg;
+        for (int s = s0; s < s1; ++s) {
+            int32_t *cs = cnt.data() + (size_t)s * h->n_cell;
+            for (int64_t i = offs[s]; i < offs[s + 1]; ++i) ++cs[d->cell[i]];
+            int64_t at = offs[s];
+            for (int c = 0; c < h->n_cell; ++c) {
+                pos[c] = at;
+                at += cs[c];
+            }
+            for (int64_t i = offs[s]; i < offs[s + 1]; ++i) perm[pos[d->cell[i]]++] = i;   // by cell, stable
+            for (int c = 0, b = 0; c < h->n_cell; b += cs[c], ++c) {
+                if (cs[c] < 2) continue;
+                int64_t *q = perm.data() + offs[s] + b;
+                seg.resize(cs[c]);
+                for (int j = 0; j < cs[c]; ++j) seg[j] = {d->rt[q[j]], q[j]};
+                std::sort(seg.begin(), seg.end());     // by RT, then data order
+                for (int j = 0; j < cs[c]; ++j) q[j] = seg[j].second;
+            }
+            for (int64_t j = offs[s]; j < offs[s + 1]; ++j) {
+                r64[j] = d->rt[perm[j]];
+                c16[j] = (uint16_t)d->cell[perm[j]];
+            }
+        }
+    };
+    const int nt = (int)std::min<int64_t>({(int64_t)std::max(1u, std::thread::hardware_concurrency()), 16,
+                                           (int64_t)std::max(S, 1), std::max<int64_t>(1, N / 20000)});
+    if (nt <= 1) {
+        sort_subjects(0, S);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t) pool.emplace_back(sort_subjects, (int)((int64_t)S * t / nt), (int)((int64_t)S * (t + 1) / nt));
+        for (auto &th : pool) th.join();
     }
     h->S = S;
     h->h_offs = offs;
@@ -460,7 +469,8 @@ ggdmc_status upload_data(ggdmc_handle *h, const ggdmc_data *d)
     cudaStream_t st = h->stream;
     CU(h->offs.upload(offs.data(), offs.size(), st));
     CU(h->rt64.upload(r64.data(), N, st));
-    CU(h->rt32.upload(r32.data(), N, st));
+    CU(h->rt32.alloc(N));
+    CU(launch_split_rt(h->rt64.p, N, h->rt32.p, st));     // (hi, lo) FP32 pairs on the device
     CU(h->cell.upload(c16.data(), N, st));
     CU(h->cell_cnt.upload(cnt.data(), cnt.size(), st));
     return wait_stream(st);
@@ -833,6 +843,14 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         int64_t per_graph = h->tuning.graph_iters > 0 ? std::min(64, h->tuning.graph_iters) : 8;
         if (gs) per_graph = std::max(1, std::atoi(gs));
         per_graph = std::min<int64_t>(per_graph, n_iter);
+        // built-in choice: a divisor of n_iter near 8 saves capturing a
+        // second graph for the remainder
+        if (!gs && h->tuning.graph_iters <= 0)
+            for (int64_t dv = per_graph; dv >= std::max<int64_t>(4, per_graph / 2); --dv)
+                if (n_iter % dv == 0) {
+                    per_graph = dv;
+                    break;
+                }
         if (flush) CU(h->flushbuf.alloc(kFlushBytes));
         std::vector<cudaEvent_t> ev_a(per_graph + 1), ev_b(per_graph + 1);
         for (auto &e : ev_a) CU(cudaEventCreate(&e));

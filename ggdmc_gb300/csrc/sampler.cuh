@@ -167,6 +167,7 @@ int diag_kmax(int n);
 cudaError_t launch_diagnostics(const double *smp, int L, int nmc, int C, int P, int start, int n, const double *probs,
                                int n_prob, double conf, int form, double *cstat, double *wcov, double *mean,
                                double *sd, double *nse, double *tse, double *quant, double *psrf, cudaStream_t st);
+cudaError_t launch_split_rt(const double *rt, int64_t n, float2 *out, cudaStream_t st);
 cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
                             cudaStream_t st);
 cudaError_t launch_loghlike(const RunDev &r, const double *phi, double *out, cudaStream_t st);

@@ -2690,6 +2690,25 @@ cudaError_t launch_summary(const double *smp, int L, int nmc, int C, int P, int 
     return cudaGetLastError();
 }
 
+// FP32 (hi, lo) split of each response time: hi = RT rounded to FP32, lo =
+// the rest rounded to FP32 (as the host would form it).
+__global__ void k_split_rt(const double *rt, int64_t n, float2 *out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = rt[i];
+        const float hi = __double2float_rn(x);
+        out[i] = make_float2(hi, __double2float_rn(x - (double)hi));
+    }
+}
+
+cudaError_t launch_split_rt(const double *rt, int64_t n, float2 *out, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+    k_split_rt<<<(unsigned)blocks, 256, 0, st>>>(rt, n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_logprior(const double *rows, int P, const double *theta, int n, double *out,
                             cudaStream_t st)
 {

@@ -40,7 +40,8 @@ def same(a, b):
     for k in ("theta", "lp", "ll", "s_theta", "s_lp", "s_ll"):
         assert np.array_equal(a[k], b[k]), k
     assert np.array_equal(a["phi_s"][0], b["phi_s"][0])
-    for k in ("accepts", "migrations", "proposals", "trial_evals"):
+    # (the work done, trial_evals, depends on the migration steps per round)
+    for k in ("accepts", "migrations", "proposals"):
         assert a["stats"][k] == b["stats"][k], k
 
 
