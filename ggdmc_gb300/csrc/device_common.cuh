@@ -308,6 +308,16 @@ __device__ __forceinline__ bool loser_s(const Ent32 &P, float th, float tl, floa
     return ok && S * 1e-8f >= ref;
 }
 
+// A trial whose response clearly precedes its non-decision time (t = RT - t0
+// below -1e-5 s): the reference form gives it the density floor, log 1e-10
+// (t <= 0).  Times within 1e-5 s of t0 are left to the FP64 form, which
+// decides the sign exactly.
+constexpr double kLogFloor = -23.025850929940456840;       // log(1e-10)
+__device__ __forceinline__ bool t_before(float2 rt, float2 t0)
+{
+    return (rt.x - t0.x) + (rt.y - t0.y) < -1e-5f;
+}
+
 // Log density of one trial in FP32 for K accumulators, the cell's entry ids
 // winner first: d = g_w * (m 2^e); returns e and log m (the caller adds
 // log g_w in FP64).  rt, t0: (hi, lo) splits.  false: use the FP64 form.

@@ -515,6 +515,7 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
 struct WarpPart {
     float h, l;
     int e, nf;
+    double fl;   // trials at the density floor: sum of log 1e-10 - log g_w (FP64)
 };
 constexpr int kWpDoubles = kGroup * 32 * (int)(sizeof(WarpPart) / sizeof(double));
 static_assert(kWpDoubles + kGroup + kGroup * sizeof(JobPart) / sizeof(double) <= kRedDoubles,
@@ -555,9 +556,16 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
         const float2 *T0 = sm.t032 + g * NT;
         float s = 0.f, cmp = 0.f;
         int e = 0, nf = 0;
+        double fl = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int c = r.cell[base + i];
             const float2 rt = r.rt32[base + i];
+            const float2 t0 = T0[sm.ct0[c]];
+            if (t_before(rt, t0)) {
+                // the floor, less the cell constant's log g_w for this trial
+                fl += kLogFloor - sm.lg[g * NE + sm.cent[c * KR]];
+                continue;
+            }
             int ex;
             float lm;
             bool good;
@@ -565,9 +573,9 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
                 int ent[K];
 #pragma unroll
                 for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
-                good = lba_ld32<K>(rt, T0[sm.ct0[c]], ent, E, ex, lm);
+                good = lba_ld32<K>(rt, t0, ent, E, ex, lm);
             } else {
-                good = lba_ld32_n(rt, T0[sm.ct0[c]], sm.cent + c * KR, KR, E, ex, lm);
+                good = lba_ld32_n(rt, t0, sm.cent + c * KR, KR, E, ex, lm);
             }
             if (good) {
                 kahan_add(s, cmp, lm);
@@ -585,8 +593,9 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
             ff_add(hh, ll, h2, l2);
             e += __shfl_down_sync(0xffffffffu, e, o);
             nf += __shfl_down_sync(0xffffffffu, nf, o);
+            fl += __shfl_down_sync(0xffffffffu, fl, o);
         }
-        if (lane == 0) wp[g * 32 + wid] = WarpPart{hh, ll, e, nf};
+        if (lane == 0) wp[g * 32 + wid] = WarpPart{hh, ll, e, nf, fl};
     }
 }
 
@@ -646,12 +655,14 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
     for (int g = wid; g < ng; g += nw) {
         float hh = 0.f, ll = 0.f;
         int ee = 0, nf = 0;
+        double fl = 0.0;
         if (sm.flag[g] == 0 && lane < nw) {
             const WarpPart p = wp[g * 32 + lane];
             hh = p.h;
             ll = p.l;
             ee = p.e;
             nf = p.nf;
+            fl = p.fl;
         }
         for (int o = 16; o > 0; o >>= 1) {
             const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
@@ -659,8 +670,9 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
             ff_add(hh, ll, h2, l2);
             ee += __shfl_down_sync(0xffffffffu, ee, o);
             nf += __shfl_down_sync(0xffffffffu, nf, o);
+            fl += __shfl_down_sync(0xffffffffu, fl, o);
         }
-        if (lane == 0) parts[g] = JobPart{hh, ll, ee, nf, 0.0};
+        if (lane == 0) parts[g] = JobPart{hh, ll, ee, nf, fl};
     }
     __syncthreads();
     bool anyfb = false;
@@ -691,10 +703,11 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
         } else {
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int c = r.cell[base + i];
+                const float2 t0 = sm.t032[g * NT + sm.ct0[c]];
                 int ex;
                 float lm;
-                if (lba_ld32_n(r.rt32[base + i], sm.t032[g * NT + sm.ct0[c]], sm.cent + c * K, K, sm.e32 + g * NE,
-                               ex, lm))
+                if (t_before(r.rt32[base + i], t0) ||
+                    lba_ld32_n(r.rt32[base + i], t0, sm.cent + c * K, K, sm.e32 + g * NE, ex, lm))
                     continue;
                 acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
             }
