@@ -147,9 +147,9 @@ __device__ __forceinline__ double lba_logdens64(double t, const int *ents, int K
 //
 // Per proposal and accumulator tuple (the host builds them in FP64):
 struct Ent32 {
-    float4 a;   // beta_h, betam_h, kappa_h, hA_h      hA = A / (2 s); the density forms
-                //                                      czm from cz and hA, not from betam
-    float4 b;   // beta_l, betam_l, kappa_l, hA_l      (low parts)
+    float4 a;   // beta_h, fe, kappa_h, hA_h      hA = A / (2 s)
+    float4 b;   // beta_l, flm, kappa_l, hA_l     (low parts); fe ln 2 + flm = log 1e-10 - log g,
+                //                                 the floor of a trial before t0 (t_before)
     float4 c;   // g_h, g_l, q_h, q_l
 };
 

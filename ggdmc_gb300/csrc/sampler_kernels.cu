@@ -379,12 +379,15 @@ __device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, in
     df_phi_pair(kap, den, qt);
     const dfl g = df_div(sd, df_mul(Ad, den)), q = df_div(qt, den);
     const dfl ab = df_mul(df_add(Ad, Bd), is), bs = df_mul(Bd, is), ha = df_mul_f(df_mul(Ad, is), 0.5f);
-    E.a = make_float4(ab.h, bs.h, kap.h, ha.h);
-    E.b = make_float4(ab.l, bs.l, kap.l, ha.l);
-    E.c = make_float4(g.h, g.l, q.h, q.l);
     const bool ok = A > 0.0 && s > 0.0 && den.h > 1e-30f && isfinite(ab.h) && isfinite(bs.h) && isfinite(kap.h) &&
                     isfinite(g.h) && isfinite(q.h) && ha.h > 0.f && g.h > 0.f;
     lg = ok ? df_to_double(df_log(g)) : 0.0;
+    // the density floor of a trial before t0 in the trial form, less log g:
+    // log 1e-10 - lg = fe ln 2 + flm (fe an integer, |flm| <= ln 2 / 2)
+    const double fx = kLogFloor - lg, fe = rint(fx * 1.4426950408889634074);
+    E.a = make_float4(ab.h, (float)fe, kap.h, ha.h);
+    E.b = make_float4(ab.l, (float)(fx - fe * kLn2), kap.l, ha.l);
+    E.c = make_float4(g.h, g.l, q.h, q.l);
     return ok;
 }
 
@@ -515,7 +518,6 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
 struct WarpPart {
     float h, l;
     int e, nf;
-    double fl;   // trials at the density floor: sum of log 1e-10 - log g_w (FP64)
 };
 constexpr int kWpDoubles = kGroup * 32 * (int)(sizeof(WarpPart) / sizeof(double));
 static_assert(kWpDoubles + kGroup + kGroup * sizeof(JobPart) / sizeof(double) <= kRedDoubles,
@@ -556,20 +558,21 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
         const float2 *T0 = sm.t032 + g * NT;
         float s = 0.f, cmp = 0.f;
         int e = 0, nf = 0;
-        double fl = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int c = r.cell[base + i];
             const float2 rt = r.rt32[base + i];
             const float2 t0 = T0[sm.ct0[c]];
-            if (t_before(rt, t0)) {
-                // the floor, less the cell constant's log g_w for this trial
-                fl += kLogFloor - sm.lg[g * NE + sm.cent[c * KR]];
-                continue;
-            }
             int ex;
             float lm;
             bool good;
-            if constexpr (K > 0) {
+            if (t_before(rt, t0)) {
+                // the density floor as the winner's tuple stores it (its log g
+                // comes with the cell constant)
+                const Ent32 &W = E[sm.cent[c * KR]];
+                ex = (int)W.a.y;
+                lm = W.b.y;
+                good = true;
+            } else if constexpr (K > 0) {
                 int ent[K];
 #pragma unroll
                 for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
@@ -593,9 +596,8 @@ __device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, 
             ff_add(hh, ll, h2, l2);
             e += __shfl_down_sync(0xffffffffu, e, o);
             nf += __shfl_down_sync(0xffffffffu, nf, o);
-            fl += __shfl_down_sync(0xffffffffu, fl, o);
         }
-        if (lane == 0) wp[g * 32 + wid] = WarpPart{hh, ll, e, nf, fl};
+        if (lane == 0) wp[g * 32 + wid] = WarpPart{hh, ll, e, nf};
     }
 }
 
@@ -655,14 +657,12 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
     for (int g = wid; g < ng; g += nw) {
         float hh = 0.f, ll = 0.f;
         int ee = 0, nf = 0;
-        double fl = 0.0;
         if (sm.flag[g] == 0 && lane < nw) {
             const WarpPart p = wp[g * 32 + lane];
             hh = p.h;
             ll = p.l;
             ee = p.e;
             nf = p.nf;
-            fl = p.fl;
         }
         for (int o = 16; o > 0; o >>= 1) {
             const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
@@ -670,9 +670,8 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
             ff_add(hh, ll, h2, l2);
             ee += __shfl_down_sync(0xffffffffu, ee, o);
             nf += __shfl_down_sync(0xffffffffu, nf, o);
-            fl += __shfl_down_sync(0xffffffffu, fl, o);
         }
-        if (lane == 0) parts[g] = JobPart{hh, ll, ee, nf, fl};
+        if (lane == 0) parts[g] = JobPart{hh, ll, ee, nf, 0.0};
     }
     __syncthreads();
     bool anyfb = false;
