@@ -788,13 +788,21 @@ __device__ void eval_slots(const RunDev &r, int l, const int *slots, int m, SubS
 
 // Store the FP32 tables of proposal slot `slot` from theta (threads of the
 // CTA in parallel over (slot, entry) are the caller's; this is one entry).
+// entry32 as a call: its double-float chain then takes no registers from the
+// kernels that build tables beside other work (the ordered resolve: 5% of a
+// sweep of the 256-subject workload)
+__device__ __noinline__ bool entry32_call(const RunDev &r, const double *theta, int u, Ent32 &E, double &lg)
+{
+    return entry32(r, theta, u, E, lg);
+}
+
 __device__ __forceinline__ void store_entry(const RunDev &r, size_t slot, const double *theta, int u)
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0;
     if (u < NE) {
         Ent32 E;
         double lg;
-        if (!entry32(r, theta, u, E, lg)) atomicOr(&r.tab_bad[slot], 1);
+        if (!entry32_call(r, theta, u, E, lg)) atomicOr(&r.tab_bad[slot], 1);
         r.tab_e[slot * NE + u] = E;
         r.tab_lg[slot * NE + u] = lg;
     } else {
