@@ -677,6 +677,30 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
     bool anyfb = false;
     for (int g = 0; g < ng; ++g) anyfb |= parts[g].nf > 0 || sm.flag[g] != 0;
     if (!anyfb) return;
+    // the list's order is the order of the atomic pushes: sort it, so that
+    // each trial's FP64 term lands in the same thread's partial sum on every
+    // run (a bitonic sort in shared memory, padded to a power of two)
+    const int fbl = *sm.fbn;
+    if (fbl > 1 && fbl <= kFbCap) {
+        int np2 = 2;
+        while (np2 < fbl) np2 <<= 1;
+        for (int i = fbl + threadIdx.x; i < np2; i += blockDim.x) sm.fb[i] = INT_MAX;
+        __syncthreads();
+        for (int k = 2; k <= np2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+                    const int x = i ^ j;
+                    if (x > i) {
+                        const int a = sm.fb[i], b = sm.fb[x];
+                        if ((a > b) == ((i & k) == 0)) {
+                            sm.fb[i] = b;
+                            sm.fb[x] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+    }
     // FP64 for the listed trials (log g_w taken back out: the cell constant
     // counts it for every trial), or for every trial of a proposal outside
     // the FP32 form's domain

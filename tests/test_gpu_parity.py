@@ -292,3 +292,24 @@ def test_invalid_inputs_are_errors():
     th, lp, ll = informative(z, 3)
     with pytest.raises(gpu.GGDMCError):
         gpu.run_subjects(cfg, model, sub, prior, th[None], lp[None], ll[None])
+
+
+def test_mixed_sums_are_the_sampler_sums_refined_only_near_zero():
+    """GGDMC_MIXED_SUMS returns the FP32 sums as the sampler forms them;
+    GGDMC_MIXED re-evaluates in FP64 only the sums whose FP32 error could
+    reach 1e-6 of their size (|sum| < 1.2 sqrt(N) + 0.03 N): the others are
+    the same numbers bit for bit, the refined ones are within 1e-12 of the
+    FP64 sums."""
+    w = synth.uneven_lba_256(n_subject=64)
+    rng = np.random.default_rng(8)
+    th = near_truth(w, 12, rng, 0.2)
+    h = gpu.Handle(w.model, w.batch)
+    sums = h.loglik(th, abi.MIXED_SUMS)
+    refined = h.loglik(th, abi.MIXED)
+    fp64 = h.loglik(th, abi.FP64)
+    n = np.diff(w.batch.offsets)[:, None] * np.ones((1, th.shape[1]))
+    near = np.abs(sums) < 1.2 * np.sqrt(n) + 0.03 * n
+    assert near.any() and (~near).any()
+    np.testing.assert_array_equal(refined[~near], sums[~near])
+    np.testing.assert_allclose(refined[near], fp64[near], rtol=1e-12, atol=1e-11)
+    assert np.all(rel(sums[~near], fp64[~near]) <= 1e-6)
