@@ -33,14 +33,18 @@ enum StatIdx { ST_PROPOSALS = 0, ST_ACCEPTS, ST_MIGRATIONS, ST_REEVALS, ST_TRIAL
 constexpr int kVariants = 8;
 
 
-// Partial log-likelihood sums of one proposal over a range of a subject's
-// trials (group_chunk): the double-float sum of the FP32 mantissa logs,
-// their binary exponents, the trials left to FP64 and the FP64 terms.
+// Partial log-likelihood sums of one proposal over a subject's trials
+// (group_chunk): the fixed-point sum (units of 2^-32) of the trials' mantissa
+// logs and FP64 terms, their binary exponents, the trials left to FP64, and
+// the FP64 sum of a proposal outside the FP32 form's domain.  Integer sums
+// are exact, so the total does not depend on how trials map to threads.
 struct JobPart {
-    float h, l;
+    long long s;
     int32_t e, nf;
     double f64;
 };
+constexpr float kFixScale = 4294967296.f;                  // 2^32
+constexpr double kFixUnit = 1.0 / 4294967296.0;            // 2^-32
 
 struct RunDev {
     // ------------------------------------------------------------ shape

@@ -80,15 +80,22 @@ __device__ __forceinline__ double block_sum(double v, double *red)
     return out;
 }
 
-// (h, l) += (h2, l2) in double-float arithmetic (Knuth's two-sum), FP32 only.
-__device__ __forceinline__ void ff_add(float &h, float &l, float h2, float l2)
+// Add one warp's integer partials (every lane's s, e, nf) to a proposal's
+// shared-memory JobPart: a shuffle reduction, then one atomic per field from
+// lane 0.  Integer addition is exact, so neither the lanes' nor the warps'
+// order changes the result.  Warp-uniform call.
+__device__ __forceinline__ void warp_flush(JobPart &p, long long s, int e, int nf)
 {
-    const float s = h + h2;
-    const float bb = s - h;
-    float e = (h - (s - bb)) + (h2 - bb);
-    e += l + l2;
-    h = s + e;
-    l = e - (h - s);
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        e += __shfl_down_sync(0xffffffffu, e, o);
+        nf += __shfl_down_sync(0xffffffffu, nf, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (s) atomicAdd(reinterpret_cast<unsigned long long *>(&p.s), (unsigned long long)s);
+        if (e) atomicAdd(&p.e, e);
+        if (nf) atomicAdd(&p.nf, nf);
+    }
 }
 
 __device__ __forceinline__ double prior_term(const double *row, double x)
@@ -510,94 +517,88 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
     for (int g = 0; g < ng; ++g) out[g] = block_sum(acc[g] + ((double)ks[g] - (double)kc[g]), sm.red);
 }
 
-// Warp partials of group_loglik's FP32 pass, in sm.red: per proposal g and
-// warp w the double-float sum (h, l) of the trials' mantissa logs (Kahan sum
-// and compensation of each thread, reduced over the warp), the sum of their
-// binary exponents and the count of trials left to FP64; then per proposal
-// the result and its FP64 count.
-struct WarpPart {
-    float h, l;
-    int e, nf;
-};
-constexpr int kWpDoubles = kGroup * 32 * (int)(sizeof(WarpPart) / sizeof(double));
-static_assert(kWpDoubles + kGroup + kGroup * sizeof(JobPart) / sizeof(double) <= kRedDoubles,
-              "sm.red holds the warp partials, the results and the job parts");
-__device__ __forceinline__ WarpPart *warp_parts(const SubSmem &sm) { return reinterpret_cast<WarpPart *>(sm.red); }
-__device__ __forceinline__ double *group_res(const SubSmem &sm) { return sm.red + kWpDoubles; }
+// group_loglik's per-proposal results and partial sums, in sm.red after the
+// 33 doubles block_sum uses.
+constexpr int kResOff = 40;
+static_assert(kResOff + kGroup + kGroup * sizeof(JobPart) / sizeof(double) <= kRedDoubles,
+              "sm.red holds block_sum's partials, the results and the job parts");
+__device__ __forceinline__ double *group_res(const SubSmem &sm) { return sm.red + kResOff; }
 __device__ __forceinline__ JobPart *job_parts(const SubSmem &sm)
 {
-    return reinterpret_cast<JobPart *>(sm.red + kWpDoubles + kGroup);
-}
-
-// Kahan-compensated FP32 accumulation (sum s, compensation c)
-__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
-{
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
+    return reinterpret_cast<JobPart *>(sm.red + kResOff + kGroup);
 }
 
 // The FP32 pass of group_loglik over trials [base, base + n) for K
-// accumulators (K = 0: the design's count at run time), one proposal at a
-// time: a thread holds one proposal's sums, which its warp reduces into
-// warp_parts once the proposal's trials are done (no per-proposal arrays;
-// every sum in a fixed order).  The subject's trial data is read once per
-// proposal (it stays in L1).  A trial the FP32 form declines is listed for
-// FP64.
+// accumulators (K = 0: the design's count at run time) and the ng proposals
+// loaded in sm, into parts[g] (zeroed by the caller).  The work is split
+// into chunks of 32 consecutive trials of one proposal, chunk c = g nch + j
+// (nch chunks per proposal), and warp w takes chunks w, w + nw, ...: every
+// warp is busy while there are chunks, whatever the number of proposals or
+// trials.  Each trial adds its mantissa log in fixed point (lm 2^32 rounded
+// to an integer; |lm| < 0.35, so it fits an int) and its binary exponent;
+// a warp adds its partials to the proposal's JobPart when it moves on to the
+// next proposal.  The sums are exact integers, so a proposal's result is
+// the same for any block size, grouping or kernel.  A trial the FP32 form
+// declines is listed for FP64.
 template <int K>
-__device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, int n, const SubSmem &sm, int ng)
+__device__ __forceinline__ void lba_group_loop32(const RunDev &r, int64_t base, int n, const SubSmem &sm, int ng,
+                                                 JobPart *parts)
 {
     const int NE = r.m.n_ent, NT = r.m.n_t0, KR = r.m.n_acc;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    WarpPart *wp = warp_parts(sm);
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int nch = (n + 31) >> 5;
+    if (nch == 0) return;
+    int g = 0, j = threadIdx.x >> 5;                 // this warp's chunk (g, j), warp-uniform
+    while (j >= nch && g < ng) { j -= nch; ++g; }
+    long long s = 0;
+    int e = 0, nf = 0;
 #pragma unroll 1
-    for (int g = 0; g < ng; ++g) {
-        if (sm.flag[g] != 0) continue;              // uniform over the block
-        const Ent32 *E = sm.e32 + g * NE;
-        const float2 *T0 = sm.t032 + g * NT;
-        float s = 0.f, cmp = 0.f;
-        int e = 0, nf = 0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int c = r.cell[base + i];
-            const float2 rt = r.rt32[base + i];
-            const float2 t0 = T0[sm.ct0[c]];
-            int ex;
-            float lm;
-            bool good;
-            if (t_before(rt, t0)) {
-                // the density floor as the winner's tuple stores it (its log g
-                // comes with the cell constant)
-                const Ent32 &W = E[sm.cent[c * KR]];
-                ex = (int)W.a.y;
-                lm = W.b.y;
-                good = true;
-            } else if constexpr (K > 0) {
-                int ent[K];
+    while (g < ng) {
+        if (sm.flag[g] == 0) {
+            const Ent32 *E = sm.e32 + g * NE;
+            const float2 *T0 = sm.t032 + g * NT;
+            const int i = (j << 5) + lane;
+            if (i < n) {
+                const int c = r.cell[base + i];
+                const float2 rt = r.rt32[base + i];
+                const float2 t0 = T0[sm.ct0[c]];
+                int ex;
+                float lm;
+                bool good;
+                if (t_before(rt, t0)) {
+                    // the density floor as the winner's tuple stores it (its log g
+                    // comes with the cell constant)
+                    const Ent32 &W = E[sm.cent[c * KR]];
+                    ex = (int)W.a.y;
+                    lm = W.b.y;
+                    good = true;
+                } else if constexpr (K > 0) {
+                    int ent[K];
 #pragma unroll
-                for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
-                good = lba_ld32<K>(rt, t0, ent, E, ex, lm);
-            } else {
-                good = lba_ld32_n(rt, t0, sm.cent + c * KR, KR, E, ex, lm);
-            }
-            if (good) {
-                kahan_add(s, cmp, lm);
-                e += ex;
-            } else {
-                ++nf;
-                const int pos = atomicAdd(sm.fbn, 1);
-                if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
+                    for (int k = 0; k < K; ++k) ent[k] = sm.cent[c * K + k];
+                    good = lba_ld32<K>(rt, t0, ent, E, ex, lm);
+                } else {
+                    good = lba_ld32_n(rt, t0, sm.cent + c * KR, KR, E, ex, lm);
+                }
+                if (good) {
+                    s += (long long)__float2int_rn(lm * kFixScale);
+                    e += ex;
+                } else {
+                    ++nf;
+                    const int pos = atomicAdd(sm.fbn, 1);
+                    if (pos < kFbCap) sm.fb[pos] = (i << 2) | g;
+                }
             }
         }
-        float hh = s, ll = -cmp;
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
-            ff_add(hh, ll, h2, l2);
-            e += __shfl_down_sync(0xffffffffu, e, o);
-            nf += __shfl_down_sync(0xffffffffu, nf, o);
+        const int g0 = g;
+        j += nw;
+        while (j >= nch && g < ng) { j -= nch; ++g; }
+        if (g != g0) {
+            warp_flush(parts[g0], s, e, nf);
+            s = 0;
+            e = 0;
+            nf = 0;
         }
-        if (lane == 0) wp[g * 32 + wid] = WarpPart{hh, ll, e, nf};
     }
 }
 
@@ -609,12 +610,14 @@ constexpr int kAnyModel = 0, kLbaOnly = 1, kDdmOnly = 2, kLba4 = 3;
 // Partial log-likelihood sums of trials [i0, i1) of subject level l for the
 // ng (<= kGroup) proposals loaded in sm, on the whole CTA, into parts[g]
 // (shared memory; valid on all threads on return).  MIXED LBA: the FP32
-// pass (lba_group_loop32) leaves per-warp partials that warp g combines for
-// proposal g; a trial's log density is log g_w + e ln 2 + log m, and log g_w
-// is NOT included here (group_cell_const adds it once per cell).  FP64
-// tables are built only for a proposal some trial of which needs the FP64
-// form, and only those trials use it; their FP64 value, less log g_w, goes
-// to parts[g].f64.  FP64 and the diffusion model: parts[g].f64 only.
+// pass (lba_group_loop32) adds each trial's binary exponent and fixed-point
+// mantissa log to parts[g]; a trial's log density is log g_w + e ln 2 +
+// log m, and log g_w is NOT included here (group_cell_const adds it once per
+// cell).  FP64 tables are built only for a proposal some trial of which
+// needs the FP64 form, and only those trials use it; their FP64 value, less
+// log g_w, is added to parts[g].s in the same fixed point (a value of 2^30
+// or more in magnitude, or not finite, to parts[g].f64).  A proposal outside
+// the FP32 form's domain, FP64 and the diffusion model: parts[g].f64 only.
 template <int MODEL = kAnyModel>
 __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed, JobPart *parts)
 {
@@ -625,7 +628,7 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
     if (ddm) {
         double o[kGroup];
         ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, o);
-        if (threadIdx.x < ng) parts[threadIdx.x] = JobPart{0.f, 0.f, 0, 0, o[threadIdx.x]};
+        if (threadIdx.x < ng) parts[threadIdx.x] = JobPart{0, 0, 0, o[threadIdx.x]};
         __syncthreads();
         return;
     }
@@ -638,69 +641,24 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
             double acc = 0.0;
             for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
             const double tot = block_sum(acc, sm.red);
-            if (threadIdx.x == 0) parts[g] = JobPart{0.f, 0.f, 0, 0, tot};
+            if (threadIdx.x == 0) parts[g] = JobPart{0, 0, 0, tot};
         }
         __syncthreads();
         return;
     }
     if (threadIdx.x == 0) *sm.fbn = 0;
+    if (threadIdx.x < ng) parts[threadIdx.x] = JobPart{0, 0, 0, 0.0};
     __syncthreads();
     switch (MODEL == kLba4 ? 4 : K) {
-    case 2: if constexpr (MODEL != kLba4) lba_group_loop32<2>(r, base, n, sm, ng); break;
-    case 3: if constexpr (MODEL != kLba4) lba_group_loop32<3>(r, base, n, sm, ng); break;
-    case 4: lba_group_loop32<4>(r, base, n, sm, ng); break;
-    default: if constexpr (MODEL != kLba4) lba_group_loop32<0>(r, base, n, sm, ng); break;
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const WarpPart *wp = warp_parts(sm);
-    for (int g = wid; g < ng; g += nw) {
-        float hh = 0.f, ll = 0.f;
-        int ee = 0, nf = 0;
-        if (sm.flag[g] == 0 && lane < nw) {
-            const WarpPart p = wp[g * 32 + lane];
-            hh = p.h;
-            ll = p.l;
-            ee = p.e;
-            nf = p.nf;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, hh, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, ll, o);
-            ff_add(hh, ll, h2, l2);
-            ee += __shfl_down_sync(0xffffffffu, ee, o);
-            nf += __shfl_down_sync(0xffffffffu, nf, o);
-        }
-        if (lane == 0) parts[g] = JobPart{hh, ll, ee, nf, 0.0};
+    case 2: if constexpr (MODEL != kLba4) lba_group_loop32<2>(r, base, n, sm, ng, parts); break;
+    case 3: if constexpr (MODEL != kLba4) lba_group_loop32<3>(r, base, n, sm, ng, parts); break;
+    case 4: lba_group_loop32<4>(r, base, n, sm, ng, parts); break;
+    default: if constexpr (MODEL != kLba4) lba_group_loop32<0>(r, base, n, sm, ng, parts); break;
     }
     __syncthreads();
     bool anyfb = false;
     for (int g = 0; g < ng; ++g) anyfb |= parts[g].nf > 0 || sm.flag[g] != 0;
     if (!anyfb) return;
-    // the list's order is the order of the atomic pushes: sort it, so that
-    // each trial's FP64 term lands in the same thread's partial sum on every
-    // run (a bitonic sort in shared memory, padded to a power of two)
-    const int fbl = *sm.fbn;
-    if (fbl > 1 && fbl <= kFbCap) {
-        int np2 = 2;
-        while (np2 < fbl) np2 <<= 1;
-        for (int i = fbl + threadIdx.x; i < np2; i += blockDim.x) sm.fb[i] = INT_MAX;
-        __syncthreads();
-        for (int k = 2; k <= np2; k <<= 1)
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = threadIdx.x; i < np2; i += blockDim.x) {
-                    const int x = i ^ j;
-                    if (x > i) {
-                        const int a = sm.fb[i], b = sm.fb[x];
-                        if ((a > b) == ((i & k) == 0)) {
-                            sm.fb[i] = b;
-                            sm.fb[x] = a;
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-    }
     // FP64 for the listed trials (log g_w taken back out: the cell constant
     // counts it for every trial), or for every trial of a proposal outside
     // the FP32 form's domain
@@ -714,6 +672,13 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
         __syncthreads();
         const int fbn = *sm.fbn;
         double acc = 0.0;
+        auto add_fixed = [&](double x) {
+            if (fabs(x) < 1073741824.0)
+                atomicAdd(reinterpret_cast<unsigned long long *>(&parts[g].s),
+                          (unsigned long long)__double2ll_rn(x * 4294967296.0));
+            else
+                acc += x;
+        };
         if (!usable) {
             for (int i = threadIdx.x; i < n; i += blockDim.x) acc += trial64(r, sm, base + i, r.cell[base + i], K);
         } else if (fbn <= kFbCap) {
@@ -721,7 +686,7 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
                 const int e = sm.fb[q];
                 if ((e & 3) != g) continue;
                 const int i = e >> 2, c = r.cell[base + i];
-                acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
+                add_fixed(trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]]);
             }
         } else {
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -732,10 +697,10 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
                 if (t_before(r.rt32[base + i], t0) ||
                     lba_ld32_n(r.rt32[base + i], t0, sm.cent + c * K, K, sm.e32 + g * NE, ex, lm))
                     continue;
-                acc += trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]];
+                add_fixed(trial64(r, sm, base + i, c, K) - sm.lg[g * NE + sm.cent[c * K]]);
             }
         }
-        const double tot = block_sum(acc, sm.red);  // red[0..32]: the warp partials are consumed
+        const double tot = block_sum(acc, sm.red);  // its barriers also order the atomics
         if (threadIdx.x == 0) parts[g].f64 += tot;
         __syncthreads();
     }
@@ -751,7 +716,7 @@ __device__ __forceinline__ double group_cell_const(const RunDev &r, int l, const
     double dc = 0.0;
     for (int c = lane; c < r.m.n_cell; c += 32) {
         const int nc = cnt[c];
-        if (nc) dc += (double)nc * lg[cent[c * K]];
+        if (nc) dc = __fma_rn((double)nc, lg[cent[c * K]], dc);
     }
     for (int o = 16; o > 0; o >>= 1) dc += __shfl_down_sync(0xffffffffu, dc, o);
     return __shfl_sync(0xffffffffu, dc, 0);
@@ -761,7 +726,9 @@ __device__ __forceinline__ double group_cell_const(const RunDev &r, int l, const
 // the FP32 form was not used).
 __device__ __forceinline__ double part_total(const JobPart &p, double dc)
 {
-    return dc + ((double)p.h + (double)p.l) + kLn2 * (double)p.e + p.f64;
+    // explicit roundings: the same value in every kernel that forms it
+    return __dadd_rn(__dadd_rn(__dadd_rn(dc, __dmul_rn((double)p.s, kFixUnit)), __dmul_rn(kLn2, (double)p.e)),
+                     p.f64);
 }
 
 // Log-likelihood sums of the subject's trials for the ng (<= kGroup)

@@ -313,3 +313,27 @@ def test_mixed_sums_are_the_sampler_sums_refined_only_near_zero():
     np.testing.assert_array_equal(refined[~near], sums[~near])
     np.testing.assert_allclose(refined[near], fp64[near], rtol=1e-12, atol=1e-11)
     assert np.all(rel(sums[~near], fp64[~near]) <= 1e-6)
+
+
+@pytest.mark.parametrize("fused", ["0", "1"])
+def test_sampler_sums_equal_the_api_sums(monkeypatch, fused):
+    """A proposal's FP32 sum is an exact integer sum of per-trial terms, so it
+    is the same number in every kernel that forms it: every log-likelihood a
+    mixed run stores (the speculative evaluation, the resolve's
+    re-evaluations, migration variants; with GGDMC_FUSED=1 the fused
+    schedule) equals GGDMC_MIXED_SUMS of its theta bit for bit."""
+    monkeypatch.setenv("GGDMC_FUSED", fused)
+    w = synth.uneven_lba_256(n_subject=24, n_lo=40, n_hi=900)
+    h = gpu.Handle(w.model, w.batch)
+    S, C, P = w.batch.n_subject, 18, w.model.n_par
+    th = near_truth(w, C, np.random.default_rng(21), 0.1)
+    lp = np.stack([gpu.logprior(w.p_prior, th[s]) for s in range(S)])
+    ll = h.loglik(th, abi.MIXED_SUMS)
+    cfg = abi.DEConfigPy(nchain=C, nparameter=P, nmc=7, thin=1, sub_migration_prob=0.3,
+                         precision=abi.MIXED, seed=31)
+    out = h.run(cfg, w.p_prior, th, lp, ll)
+    st = out["stats"]
+    assert st["reevaluations"] > 0 and st["migrations"] > 0 and st["accepts"] > 0
+    smp = out["s_theta"].reshape(S, -1, P)                 # every stored sample
+    np.testing.assert_array_equal(h.loglik(smp, abi.MIXED_SUMS), out["s_ll"].reshape(S, -1))
+    np.testing.assert_array_equal(h.loglik(out["theta"], abi.MIXED_SUMS), out["ll"])
