@@ -181,7 +181,8 @@ struct ggdmc_handle {
     DevBuf<double> th, lp, ll, th_s, lp_s, ll_s, phi_tab, pp_bounds, prior, hprior, hrows;
     DevBuf<double> pth, plp, pll, pth_s, plp_s, pll_s, pref_src, pref_next;
     DevBuf<int32_t> partner, ptype, nstep, sub, migrated, ppartner, pptype, pnstep, psub,
-        pmigrated, iter, status, items, items_plain, rs_para, sub_order, ready, spec_cnt, ctl;
+        pmigrated, iter, status, items, items_plain, rs_para, sub_order, res_order, lvl_ns, ready, spec_cnt,
+        ctl;
     DevBuf<int8_t> need, pneed;
     DevBuf<Ent32> tab_e;
     DevBuf<double> tab_lg;
@@ -626,6 +627,9 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
         CU(h->items.upload(items.data(), items.size(), st));
         CU(h->items_plain.upload(plain.data(), plain.size(), st));
         CU(h->sub_order.upload(order.data(), order.size(), st));
+        CU(h->res_order.upload(order.data(), order.size(), st));
+        CU(h->lvl_ns.alloc(S));
+        CU(cudaMemsetAsync(h->lvl_ns.p, 0, sizeof(int32_t) * S, st));
     }
     if (Pphi > 0) {
         CU(h->pth.alloc((size_t)C * Pphi));
@@ -720,6 +724,8 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     r.cell_cnt = h->cell_cnt.p;
     r.rs_para = h->rs_para.p; r.CS = CS;
     r.sub_order = h->sub_order.p;
+    r.res_order = h->res_order.p;
+    r.lvl_ns = h->lvl_ns.p;
     r.pjit = h->pjit.p; r.paccu = h->paccu.p;
     r.prior = (!hier && !hyper) ? h->prior.p : nullptr;
     r.pp_bounds = (hier || hyper) ? h->pp_bounds.p : nullptr;
@@ -787,6 +793,12 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             if (hier) {
                 if ((e = launch_phi_tables(r, st))) return e;
                 ++launches_per_iter;
+                // the resolve's level order (used when its levels take more
+                // than one wave), beside the speculative evaluation
+                if (fork && !fused && S > h->n_sm) {
+                    if ((e = launch_level_order(r, st))) return e;
+                    ++launches_per_iter;
+                }
             }
         }
         if (S > 0) {

@@ -62,6 +62,13 @@ constexpr int kCtlResNext = 0, kCtlResDone = 1, kCtlEvents = 2, kCtlN = 3;
 constexpr int kPhiProposeThreads = 1024;   // one CTA: a warp per phi chain's prior
 
 // ------------------------------------------------------------- helpers
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ double block_sum(double v, double *red)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -1294,6 +1301,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
     const size_t lc = (size_t)l * C, ls = (size_t)l * r.CS;
     const bool mixed = r.prec == PREC_MIXED;
     ResSmem rs = carve_res(smem_raw + sub_smem_bytes(r.m), C);
+    const unsigned long long t_beg = (threadIdx.x == 0) ? global_ns() : 0ull;
     if (score_priors) {
         // deferred priors of the pass's proposals (and migration cascade),
         // with the phi chains of this sweep: a warp per slot
@@ -1396,8 +1404,10 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                 }
             }
             if (mixed) {
+                // from the block's last thread down, so the tables build on
+                // other warps than the priors' (warps 0..m-1), at the same time
                 const int NU = r.m.n_ent + r.m.n_t0;
-                for (int q = ct; q < m * NU; q += cstride) {
+                for (int q = cstride - 1 - ct; q < m * NU; q += cstride) {
                     const int k = rs.list[q / NU];
                     store_entry(r, ls + k, r.th_s + (ls + k) * P, q % NU);
                 }
@@ -1452,36 +1462,34 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                     // (score a^c, 2 for c = 0); c >= kVariants: the value for
                     // step rj + 1 + k after a reject at rj = d + (c - kVariants) / 3,
                     // k = 1 + (c - kVariants) % 3 (score (1 - a) a^k 0.95^(rj - d));
-                    // the mig_round best, ties to the lower c
+                    // the mig_round best, ties to the lower c.  Scores are
+                    // ranked as FP32 log2 values: they only choose which values
+                    // are evaluated ahead, never a result.
                     const int c = threadIdx.x;
-                    const double a = (rs.misc[5] + 1.0) / (d + 2.0);
-                    double sc = -1.0;
+                    const float a = (rs.misc[5] + 1.f) / (d + 2.f);       // in (0, 1)
+                    const float la = __log2f(a), lb = __log2f(1.f - a);
+                    float sc = -INFINITY;
                     int vr = 0, vs = 0;
                     if (c < kVariants) {
                         if (d + c < n) {
-                            double ak = 1.0;
-                            for (int k = 0; k < c; ++k) ak *= a;
-                            sc = (c == 0) ? 2.0 : ak;
+                            sc = (c == 0) ? 1.f : (float)c * la;
                             vr = -1;
                             vs = d + c;
                         }
                     } else {
                         const int rj = d + (c - kVariants) / 3, k = 1 + (c - kVariants) % 3;
                         if (rj + 1 + k < n) {
-                            double v = 1.0 - a;
-                            for (int q = 0; q < k; ++q) v *= a;
-                            for (int q = d; q < rj; ++q) v *= 0.95;
-                            sc = v;
+                            sc = fmaf((float)(rj - d), -0.0740005815f, fmaf((float)k, la, lb));   // log2 0.95
                             vr = rj;
                             vs = rj + 1 + k;
                         }
                     }
                     int rank = 0;
                     for (int o = 0; o < 32; ++o) {
-                        const double so = __shfl_sync(0xffffffffu, sc, o);
+                        const float so = __shfl_sync(0xffffffffu, sc, o);
                         rank += (so > sc || (so == sc && o < c)) ? 1 : 0;
                     }
-                    const bool valid = sc > 0.0;
+                    const bool valid = sc > -INFINITY;
                     if (valid && rank < mig_round) {
                         rs.vr[rank] = vr;
                         rs.vs[rank] = vs;
@@ -1510,8 +1518,8 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
                     }
                 }
                 if (mixed) {
-                    const int NU = r.m.n_ent + r.m.n_t0;
-                    for (int q = ct; q < nv * NU; q += cstride) {
+                    const int NU = r.m.n_ent + r.m.n_t0;              // beside the priors' warps
+                    for (int q = cstride - 1 - ct; q < nv * NU; q += cstride) {
                         const int w = q / NU;
                         store_entry(r, ls + C + w, r.th_s + (ls + C + w) * P, q % NU);
                     }
@@ -1574,6 +1582,12 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
         }
     }
     if (threadIdx.x == 0) {
+        // this level's cost, for the order of the next sweep's crossover
+        // levels: the mean of the last measurement and the one before
+        if (type == PASS_CROSS) {
+            const long long t = (long long)min(global_ns() - t_beg, 0x7fffffffull), o = r.lvl_ns[l];
+            r.lvl_ns[l] = (int32_t)(o > 0 ? (o + t) / 2 : t);
+        }
         atomicAdd(&r.stats[ST_PROPOSALS], (unsigned long long)n);
         atomicAdd(&r.stats[ST_REEVALS], (unsigned long long)reevals);
         atomicAdd(&r.stats[ST_VARIANTS], (unsigned long long)variants);
@@ -1583,7 +1597,7 @@ __device__ void resolve_level(const RunDev &r, int l, SubSmem &sm, char *smem_ra
 
 // The level at rank q of the order the resolve takes levels in: this pass's
 // migration levels (the longest to resolve: a round per few steps) first,
-// then the others, each group in sub_order's order (largest first).  All
+// then the others, each group in res_order's order (k_level_order).  All
 // threads; tmp holds 34 ints.
 __device__ int mig_first_level(const RunDev &r, int q, int *tmp)
 {
@@ -1591,7 +1605,7 @@ __device__ int mig_first_level(const RunDev &r, int q, int *tmp)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     // number of migration levels
     int c = 0;
-    for (int i = threadIdx.x; i < S; i += blockDim.x) c += r.ptype[r.sub_order[i]] == PASS_MIG;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) c += r.ptype[r.res_order[i]] == PASS_MIG;
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
     if (threadIdx.x == 0) tmp[33] = 0;
     __syncthreads();
@@ -1604,7 +1618,7 @@ __device__ int mig_first_level(const RunDev &r, int q, int *tmp)
     int found = -1;
     for (int b0 = 0; b0 < S && found < 0; b0 += blockDim.x) {
         const int i = b0 + threadIdx.x;
-        const bool p = i < S && ((r.ptype[r.sub_order[i]] == PASS_MIG) == want);
+        const bool p = i < S && ((r.ptype[r.res_order[i]] == PASS_MIG) == want);
         const unsigned m = __ballot_sync(0xffffffffu, p);
         if (lane == 0) tmp[wid] = __popc(m);
         __syncthreads();
@@ -1616,7 +1630,7 @@ __device__ int mig_first_level(const RunDev &r, int q, int *tmp)
         }
         __syncthreads();
         const int before = tmp[wid] + __popc(m & ((1u << lane) - 1u));
-        if (p && before == rank) tmp[33] = r.sub_order[i];
+        if (p && before == rank) tmp[33] = r.res_order[i];
         const int total = tmp[32];
         __syncthreads();
         found = tmp[33];
@@ -2191,6 +2205,29 @@ __global__ void k_phi_tables(RunDev r)
     }
 }
 
+// k_level_order: the order of the next k_sub_resolve's levels, by the
+// duration of each level's last crossover resolve, longest first (levels not
+// yet measured, and ties, in sub_order's order), so that a level slow for
+// its trial count (many rounds, FP64 fallbacks) starts in the first wave.
+// One block; a level's rank is the count of larger keys.  Runs beside the
+// subject kernels (after the phi level), off the sweep's critical path.
+constexpr int kOrderMax = 4096;
+__global__ void k_level_order(RunDev r)
+{
+    __shared__ unsigned long long key[kOrderMax];
+    const int S = r.S;
+    if (S > kOrderMax) return;                   // keep the order as it is
+    for (int q = threadIdx.x; q < S; q += blockDim.x)
+        key[q] = ((unsigned long long)(unsigned)max(r.lvl_ns[r.sub_order[q]], 0) << 32) | (unsigned)(S - 1 - q);
+    __syncthreads();
+    for (int q = threadIdx.x; q < S; q += blockDim.x) {
+        const unsigned long long k = key[q];
+        int rank = 0;
+        for (int j = 0; j < S; ++j) rank += key[j] > k ? 1 : 0;
+        r.res_order[rank] = r.sub_order[q];
+    }
+}
+
 // k_store: theta_class::store (thinned copy of the state into the samples).
 __global__ void k_store(RunDev r)
 {
@@ -2543,6 +2580,12 @@ cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int l
 cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st)
 {
     k_phi_tables<<<r.C, 32, 0, st>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level_order(const RunDev &r, cudaStream_t st)
+{
+    k_level_order<<<1, 256, 0, st>>>(r);
     return cudaGetLastError();
 }
 
