@@ -312,7 +312,6 @@ __device__ __forceinline__ bool loser_s(const Ent32 &P, float th, float tl, floa
 // below -1e-5 s): the reference form gives it the density floor, log 1e-10
 // (t <= 0).  Times within 1e-5 s of t0 are left to the FP64 form, which
 // decides the sign exactly.
-constexpr double kLogFloor = -23.025850929940456840;       // log(1e-10)
 __device__ __forceinline__ bool t_before(float2 rt, float2 t0)
 {
     return (rt.x - t0.x) + (rt.y - t0.y) < -1e-5f;

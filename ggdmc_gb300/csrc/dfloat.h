@@ -95,14 +95,27 @@ GG_HD dfl df_mul_f(dfl a, float b)
     return df_fast_two_sum(p, e);
 }
 
-// a / b: FP32 quotient, then one correction with the exact remainder
+// 1 / x in FP32, correctly rounded (the quotients below only need it to a
+// few ulps: each is corrected with an exact remainder)
+GG_HD float df_rcp(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(x);
+#else
+    return 1.f / x;
+#endif
+}
+
+// a / b: three FP32 quotients from one reciprocal of b.h, each correcting
+// the exact remainder of the ones before (a - b q1, then a - b (q1 + q2))
 GG_HD dfl df_div(dfl a, dfl b)
 {
-    const float q1 = a.h / b.h;
+    const float rb = df_rcp(b.h);
+    const float q1 = a.h * rb;
     const dfl r = df_add(a, df_neg(df_mul_f(b, q1)));     // a - b q1
-    const float q2 = r.h / b.h;
+    const float q2 = r.h * rb;
     const dfl r2 = df_add(r, df_neg(df_mul_f(b, q2)));
-    const float q3 = r2.h / b.h;
+    const float q3 = r2.h * rb;
     dfl q = df_fast_two_sum(q1, q2);
     return df_add_f(q, q3);
 }

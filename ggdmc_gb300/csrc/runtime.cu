@@ -676,15 +676,16 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
     CU(cudaMemsetAsync(h->status.p, 0, sizeof(int32_t), st));
     // The subject pass fused with the next iteration's proposals
     // (k_sub_step) needs one subject pass per iteration and not the plain
-    // form.  It pays where the levels come in several waves per SM and no
-    // phi level waits for the pass: the next iteration's evaluations then
-    // fill the SMs the ordered decisions leave idle.  With a phi level the
-    // phi update of t + 1 can only start after the whole pass, and the
-    // speculative evaluations already run beside it.  GGDMC_FUSED=0/1
-    // overrides the choice.
+    // form.  It pays where the levels come in more than one wave: the next
+    // iteration's proposals and evaluations then fill the SMs the ordered
+    // decisions leave idle.  Many independent fits: from two waves per SM.
+    // Hierarchical: from one wave (the 256-subject workload: 0.823 ms per
+    // sweep against 0.844 for the ordered resolve); the rest of the
+    // speculative evaluations runs beside the phi update of t + 1.
+    // GGDMC_FUSED=0/1 overrides the choice.
     const int sub_npass = hier ? (c.is_pblocked ? c.nparameter / 2 : 1) : (c.is_pblocked ? c.nparameter : 1);
     const bool fusable = S > 0 && !plain && sub_npass == 1;
-    bool fused = fusable && !hier && Pphi == 0 && S >= 2 * h->n_sm;
+    bool fused = fusable && (hier ? S > h->n_sm : (Pphi == 0 && S >= 2 * h->n_sm));
     if (const char *fs = std::getenv("GGDMC_FUSED")) fused = fusable && std::atoi(fs) != 0;
     if (fused) {
         CU(h->ready.alloc(S));
@@ -793,10 +794,10 @@ ggdmc_status run_impl(ggdmc_handle *h, const RunArgs &a)
             if (hier) {
                 if ((e = launch_phi_tables(r, st))) return e;
                 ++launches_per_iter;
-                // the resolve's level order (used when its levels take more
-                // than one wave), beside the speculative evaluation
-                if (fork && !fused && S > h->n_sm) {
-                    if ((e = launch_level_order(r, st))) return e;
+                // the subject pass's level order (it matters when its levels
+                // take more than one wave), beside the speculative evaluation
+                if (fork && S > h->n_sm) {
+                    if ((e = launch_level_order(r, fused, st))) return e;
                     ++launches_per_iter;
                 }
             }

@@ -85,7 +85,7 @@ struct RunDev {
     double *accu;                  // [S][C]    Metropolis accept uniforms of the pass
     int32_t *rs_para;              // [S] blocked parameter of the pass, -1 for all
     const int32_t *sub_order;      // [S] subjects by trial count, largest first
-    int32_t *res_order;            // [S] k_sub_resolve's order: by the last crossover resolve's time
+    int32_t *res_order;            // [S] the subject pass's level order (k_level_order)
     int32_t *lvl_ns;               // [S] duration of each level's last crossover resolve (ns)
     int32_t CS;                    // proposal slots per level: C speculative + C variants
     // FP32 tables of every proposal slot, built where the proposal is built
@@ -143,7 +143,7 @@ cudaError_t launch_sub_loglik(const RunDev &r, const int32_t *items, int n_items
 cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int level_count,
                                bool score_priors, cudaStream_t st);
 cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st);
-cudaError_t launch_level_order(const RunDev &r, cudaStream_t st);
+cudaError_t launch_level_order(const RunDev &r, bool with_type, cudaStream_t st);
 cudaError_t launch_phi_propose(const RunDev &r, int pass, cudaStream_t st);
 cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st);
 cudaError_t launch_phi_resolve(const RunDev &r, int pass, cudaStream_t st);

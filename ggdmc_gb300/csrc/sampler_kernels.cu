@@ -393,14 +393,19 @@ __device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, in
     df_phi_pair(kap, den, qt);
     const dfl g = df_div(sd, df_mul(Ad, den)), q = df_div(qt, den);
     const dfl ab = df_mul(df_add(Ad, Bd), is), bs = df_mul(Bd, is), ha = df_mul_f(df_mul(Ad, is), 0.5f);
-    const bool ok = A > 0.0 && s > 0.0 && den.h > 1e-30f && isfinite(ab.h) && isfinite(bs.h) && isfinite(kap.h) &&
-                    isfinite(g.h) && isfinite(q.h) && ha.h > 0.f && g.h > 0.f;
-    lg = ok ? df_to_double(df_log(g)) : 0.0;
+    // (FP32 tests of A and s: a value too small for FP32 goes to the FP64 form)
+    const bool ok = Ad.h > 0.f && sd.h > 0.f && den.h > 1e-30f && isfinite(ab.h) && isfinite(bs.h) &&
+                    isfinite(kap.h) && isfinite(g.h) && isfinite(q.h) && ha.h > 0.f && g.h > 0.f;
+    const dfl lgd = ok ? df_log(g) : dfl{0.f, 0.f};
+    lg = df_to_double(lgd);
     // the density floor of a trial before t0 in the trial form, less log g:
-    // log 1e-10 - lg = fe ln 2 + flm (fe an integer, |flm| <= ln 2 / 2)
-    const double fx = kLogFloor - lg, fe = rint(fx * 1.4426950408889634074);
-    E.a = make_float4(ab.h, (float)fe, kap.h, ha.h);
-    E.b = make_float4(ab.l, (float)(fx - fe * kLn2), kap.l, ha.l);
+    // log 1e-10 - log g = fe ln 2 + flm (fe an integer, |flm| <= ln 2 / 2),
+    // in double-float (log 1e-10 as hi + lo)
+    const dfl fx = df_add(dfl{-23.025850296020508f, -6.339199671856477e-07f}, df_neg(lgd));
+    const float fe = rintf(fx.h * 1.44269504088896341f);
+    const dfl fl = df_add(fx, df_neg(df_mul_f(dfl{kDfLn2H, kDfLn2L}, fe)));
+    E.a = make_float4(ab.h, fe, kap.h, ha.h);
+    E.b = make_float4(ab.l, fl.h + fl.l, kap.l, ha.l);
     E.c = make_float4(g.h, g.l, q.h, q.l);
     return ok;
 }
@@ -1660,7 +1665,7 @@ k_sub_resolve(RunDev r, int level_begin, int n_level, int ordered, int score_pri
 }
 
 // k_sub_step: the subject pass of iteration t (= *iter) and the start of
-// iteration t + 1's, on a persistent grid.  CTAs claim levels largest first
+// iteration t + 1's, on a persistent grid.  CTAs claim levels in res_order
 // and resolve them; the CTA that resolved level l then builds l's proposals
 // for t + 1 (they read only l's state) and publishes them (ready[l] = t + 1).
 // Once every level is claimed, CTAs evaluate spec items of published levels
@@ -1691,7 +1696,7 @@ k_sub_step(RunDev r, int score_priors, int defer_next, int group)
         const int q = s_q;
         __syncthreads();
         if (q >= r.S) break;
-        const int l = r.sub_order[q];
+        const int l = r.res_order[q];
         resolve_level(r, l, sm, smem_raw, score_priors != 0);
         __syncthreads();
         if (next) {
@@ -2205,20 +2210,27 @@ __global__ void k_phi_tables(RunDev r)
     }
 }
 
-// k_level_order: the order of the next k_sub_resolve's levels, by the
+// k_level_order: the order of the next subject pass's levels, by the
 // duration of each level's last crossover resolve, longest first (levels not
 // yet measured, and ties, in sub_order's order), so that a level slow for
 // its trial count (many rounds, FP64 fallbacks) starts in the first wave.
-// One block; a level's rank is the count of larger keys.  Runs beside the
+// with_type (the fused schedule, whose pass types are final here): this
+// pass's migration levels first, as k_sub_step claims levels in this order;
+// otherwise k_sub_resolve puts them first itself (mig_first_level).  One
+// block; a level's rank is the count of larger keys.  Runs beside the
 // subject kernels (after the phi level), off the sweep's critical path.
 constexpr int kOrderMax = 4096;
-__global__ void k_level_order(RunDev r)
+__global__ void k_level_order(RunDev r, int with_type)
 {
     __shared__ unsigned long long key[kOrderMax];
     const int S = r.S;
     if (S > kOrderMax) return;                   // keep the order as it is
-    for (int q = threadIdx.x; q < S; q += blockDim.x)
-        key[q] = ((unsigned long long)(unsigned)max(r.lvl_ns[r.sub_order[q]], 0) << 32) | (unsigned)(S - 1 - q);
+    for (int q = threadIdx.x; q < S; q += blockDim.x) {
+        const int l = r.sub_order[q];
+        const unsigned long long mig = (with_type && r.ptype[l] == PASS_MIG) ? 1ull : 0ull;
+        key[q] = (mig << 62) | ((unsigned long long)(unsigned)max(r.lvl_ns[l], 0) << 20) |
+                 (unsigned long long)(S - 1 - q);
+    }
     __syncthreads();
     for (int q = threadIdx.x; q < S; q += blockDim.x) {
         const unsigned long long k = key[q];
@@ -2583,9 +2595,9 @@ cudaError_t launch_phi_tables(const RunDev &r, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_level_order(const RunDev &r, cudaStream_t st)
+cudaError_t launch_level_order(const RunDev &r, bool with_type, cudaStream_t st)
 {
-    k_level_order<<<1, 256, 0, st>>>(r);
+    k_level_order<<<1, 256, 0, st>>>(r, with_type ? 1 : 0);
     return cudaGetLastError();
 }
 

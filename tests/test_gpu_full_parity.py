@@ -10,7 +10,7 @@ oracle's sequential run (src/de.cpp:272-383) given the same keyed draws:
 * migration at the workload's rates (0.05 phi, 0.06 subjects) and raised to
   0.3 for both levels, so that dozens of subjects migrate in one pass;
 * the ordered resolve (GGDMC_FUSED=0) and the persistent fused schedule
-  (GGDMC_FUSED=1, which the runtime picks by itself only for many fits);
+  (GGDMC_FUSED=1, which the runtime picks by itself for this workload);
 * host-fed draws (the canonical draw array of include/ggdmc_gpu.h) for
   ``ggdmc_run`` on the full workload and for ``ggdmc_run_hyper``.
 

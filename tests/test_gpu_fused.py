@@ -1,7 +1,8 @@
 """The subject pass fused with the next iteration's proposals (k_sub_step and
 k_sub_spec_rest) against the oracle, through the C ABI.  The runtime takes
-the fused schedule by itself only for many independent fits (at least two
-waves of levels per SM); GGDMC_FUSED=1 forces it here on small cases, with
+the fused schedule by itself for many independent fits (at least two waves
+of levels per SM) and for hierarchical runs of more than one wave;
+GGDMC_FUSED=1 forces it here on small cases, with
 and without a phi level, in CUDA-graph replays and in the iterations
 launched one by one after the last whole graph."""
 import numpy as np
