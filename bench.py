@@ -177,10 +177,11 @@ def profiled_traffic():
 
 
 def loglik_roofline(w, h, n_launch=10, precision=abi.MIXED_SUMS):
-    """Time the likelihood kernel live (CUDA events on its stream): all
-    subjects x 51 proposals per launch, the k_sub_loglik work of one sweep.
-    MIXED_SUMS times the FP32 kernel alone (the sums the sampler uses);
-    MIXED adds the likelihood API's FP64 pass over sums near zero."""
+    """Time the likelihood API's launches live (CUDA events on its stream):
+    all subjects x 51 proposals per call, the k_sub_loglik work of one sweep,
+    as k_batch_tables (the proposals' FP32 tables) then k_loglik_batch.
+    MIXED_SUMS times these two alone (the sums the sampler uses); MIXED adds
+    the likelihood API's FP64 pass over sums near zero."""
     import torch
     rng = np.random.default_rng(5)
     th, _ = synth.start_states(w, w.nchain, rng)
@@ -425,7 +426,7 @@ def run_ours(args):
         "acceptance": round(st["accepts"] / max(st["proposals"], 1), 4),
         "gpu_launches": int(st["kernel_launches"]),
         "tuning": tune_line,
-        "roofline": {"kernel": "loglik (k_loglik_batch = k_sub_loglik body)",
+        "roofline": {"kernel": "loglik (k_batch_tables + k_loglik_batch, the k_sub_loglik body)",
                      "bound": "fp32", "achieved": round(ach_tflops, 3),
                      "peak": round(peak_fp32, 3), "unit": "TFLOP/s",
                      "frac": round(ach_tflops / peak_fp32, 4), "traffic": profiled_traffic(),

@@ -193,6 +193,10 @@ struct ggdmc_handle {
     DevBuf<double> smp_th, smp_lp, smp_ll, psmp_th, psmp_lp, psmp_ll, draws;
     DevBuf<unsigned long long> stats;
     DevBuf<double> io_a, io_b;
+    DevBuf<Ent32> bt_e;                   // the likelihood batch's FP32 tables (k_batch_tables)
+    DevBuf<double> bt_lg;
+    DevBuf<float2> bt_t;
+    DevBuf<int32_t> bt_bad;
     DevBuf<int32_t> ref_count, ref_base, ref_item;   // FP64 refinement of MIXED sums near zero
     DevBuf<double> ref_partial;
     DevBuf<uint8_t> flushbuf;
@@ -1374,7 +1378,16 @@ static ggdmc_status loglik_launch(ggdmc_handle *h, const double *d_theta, int n_
                                   double *d_out, cudaStream_t st)
 {
     RunDev r = loglik_desc(h, precision);
-    CU(launch_loglik_batch(r, d_theta, n_theta, d_out, st));
+    BatchTables bt{nullptr, nullptr, nullptr, nullptr};
+    if (r.prec == PREC_MIXED && h->model_type != GGDMC_MODEL_DDM) {
+        const size_t nq = (size_t)h->S * n_theta;
+        CU(h->bt_e.alloc(nq * h->n_ent));
+        CU(h->bt_lg.alloc(nq * h->n_ent));
+        CU(h->bt_t.alloc(nq * std::max(h->n_t0, 1)));
+        CU(h->bt_bad.alloc(nq));
+        bt = BatchTables{h->bt_e.p, h->bt_lg.p, h->bt_t.p, h->bt_bad.p};
+    }
+    CU(launch_loglik_batch(r, d_theta, n_theta, d_out, st, &bt));
     if (precision != GGDMC_MIXED) return GGDMC_OK;
     const size_t cap = refine_capacity(h->h_offs.data(), h->S, n_theta);
     CU(h->ref_count.alloc(1));

@@ -149,8 +149,17 @@ cudaError_t launch_phi_eval(const RunDev &r, cudaStream_t st);
 cudaError_t launch_phi_resolve(const RunDev &r, int pass, cudaStream_t st);
 cudaError_t launch_store(const RunDev &r, cudaStream_t st);
 cudaError_t launch_next_iter(const RunDev &r, cudaStream_t st);
+// The FP32 tables of the batch's proposals ([S * n_theta] proposals), built
+// by a whole-GPU kernel before the likelihood kernel reads them (MIXED LBA);
+// nullptr pointers: each likelihood block builds its proposal's own.
+struct BatchTables {
+    Ent32 *e;        // [S * n_theta][n_ent]
+    double *lg;      // [S * n_theta][n_ent]
+    float2 *t;       // [S * n_theta][n_t0]
+    int32_t *bad;    // [S * n_theta]
+};
 cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_theta, double *out,
-                                cudaStream_t st);
+                                cudaStream_t st, const BatchTables *tabs = nullptr);
 cudaError_t launch_trial_logdens(const RunDev &r, const double *theta, double *out,
                                  cudaStream_t st);
 // FP64 refinement of the MIXED sums out [S][n_theta] near zero (theta as given

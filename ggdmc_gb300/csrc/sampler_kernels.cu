@@ -2276,20 +2276,57 @@ __global__ void k_next_iter(RunDev r)
 
 // ------------------------------------------------- batch likelihood API
 // theta [S][n_theta][P] -> out [S][n_theta]; grid = S * n_theta.
+// k_batch_tables: the FP32 tables of every proposal of a likelihood batch,
+// one thread per (proposal, tuple or t0 entry) over the whole GPU.  Built in
+// each likelihood block instead, a proposal's tuples keep a few of the
+// block's threads busy for the whole double-float chain while the others
+// wait (about 15% of the likelihood kernel's time).  bad[] is zeroed first.
+__global__ void k_batch_tables(RunDev r, const double *theta, int n_theta, BatchTables bt)
+{
+    const int NE = r.m.n_ent, NT = r.m.n_t0, NU = NE + NT;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)r.S * n_theta * NU) return;
+    const size_t q = i / NU;
+    const int u = (int)(i % NU);
+    const double *th = theta + q * r.P;
+    if (u < NE) {
+        Ent32 E;
+        double lg;
+        if (!entry32(r, th, u, E, lg)) atomicOr(bt.bad + q, 1);
+        bt.e[q * NE + u] = E;
+        bt.lg[q * NE + u] = lg;
+    } else {
+        bt.t[q * NT + (u - NE)] = t0split(r, th, u - NE);
+    }
+}
+
 template <int MINB, int MODEL>
 __global__ void __launch_bounds__(kLikThreads, MINB) k_loglik_batch(RunDev r, const double *theta,
-                                                                    int n_theta, double *out)
+                                                                    int n_theta, double *out, BatchTables bt)
 {
     extern __shared__ __align__(16) char smem_raw[];
     const int l = blockIdx.x / n_theta, k = blockIdx.x % n_theta;
+    const size_t q = (size_t)l * n_theta + k;
     SubSmem sm = carve(smem_raw, r.m);
-    const double *th = theta + ((size_t)l * n_theta + k) * r.P;
+    const double *th = theta + q * r.P;
     for (int j = threadIdx.x; j < r.P; j += blockDim.x) sm.theta[j] = th[j];
     load_design(r, sm);
-    if (threadIdx.x == 0) sm.flag[0] = 0;
-    __syncthreads();
     const bool mixed = r.prec == PREC_MIXED;
-    if (mixed) build_tables32(r, sm, 0);
+    if (mixed && bt.e) {
+        // the tables k_batch_tables built, as float4 words (3 per tuple)
+        const int NE = r.m.n_ent, NT = r.m.n_t0;
+        const float4 *src = reinterpret_cast<const float4 *>(bt.e + q * NE);
+        float4 *dst = reinterpret_cast<float4 *>(sm.e32);
+        for (int u = threadIdx.x; u < 3 * NE; u += blockDim.x) dst[u] = src[u];
+        for (int u = threadIdx.x; u < NE; u += blockDim.x) sm.lg[u] = bt.lg[q * NE + u];
+        for (int u = threadIdx.x; u < NT; u += blockDim.x) sm.t032[u] = bt.t[q * NT + u];
+        if (threadIdx.x == 0) sm.flag[0] = bt.bad[q];
+        __syncthreads();
+    } else {
+        if (threadIdx.x == 0) sm.flag[0] = 0;
+        __syncthreads();
+        if (mixed) build_tables32(r, sm, 0);
+    }
     double ll[kGroup];
     group_loglik<MODEL>(r, l, sm, 1, mixed, ll);
     if (threadIdx.x == 0) out[(size_t)l * n_theta + k] = ll[0];
@@ -2632,15 +2669,24 @@ cudaError_t launch_next_iter(const RunDev &r, cudaStream_t st)
 }
 
 cudaError_t launch_loglik_batch(const RunDev &r, const double *theta, int n_theta, double *out,
-                                cudaStream_t st)
+                                cudaStream_t st, const BatchTables *tabs)
 {
     const size_t smem = sub_smem_bytes(r.m);
+    BatchTables bt{nullptr, nullptr, nullptr, nullptr};
+    if (tabs && r.prec == PREC_MIXED && r.m.model_type != kModelDdm) {
+        bt = *tabs;
+        cudaError_t e = cudaMemsetAsync(bt.bad, 0, sizeof(int32_t) * (size_t)r.S * n_theta, st);
+        if (e) return e;
+        const size_t n = (size_t)r.S * n_theta * (r.m.n_ent + r.m.n_t0);
+        k_batch_tables<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(r, theta, n_theta, bt);
+        if ((e = cudaGetLastError())) return e;
+    }
     if (r.m.model_type == kModelDdm)
-        k_loglik_batch<GGDMC_LIK_MINB, kDdmOnly><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out);
+        k_loglik_batch<GGDMC_LIK_MINB, kDdmOnly><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out, bt);
     else if (r.m.n_acc == 4)
-        k_loglik_batch<GGDMC_LIK_MINB_LBA, kLba4><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out);
+        k_loglik_batch<GGDMC_LIK_MINB_LBA, kLba4><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out, bt);
     else
-        k_loglik_batch<GGDMC_LIK_MINB, kLbaOnly><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out);
+        k_loglik_batch<GGDMC_LIK_MINB, kLbaOnly><<<r.S * n_theta, kLikThreads, smem, st>>>(r, theta, n_theta, out, bt);
     return cudaGetLastError();
 }
 
