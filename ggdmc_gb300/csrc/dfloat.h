@@ -36,7 +36,10 @@ struct dfl {
 
 GG_HD dfl df_make(float h, float l = 0.f) { return dfl{h, l}; }
 
-// exact split of a double into hi + lo (to the FP32 resolution of lo)
+// exact split of a double into hi + lo (to the FP32 resolution of lo).
+// (An integer form of the split, without FP64 instructions, gave the same
+// bits but made the sweep 0.6% slower: four FP64 operations per parameter
+// cost less than its 64-bit integer sequence.)
 GG_HD dfl df_from_double(double x)
 {
     const float h = (float)x;

@@ -412,9 +412,8 @@ __device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, in
 
 __device__ __forceinline__ float2 t0split(const RunDev &r, const double *theta, int q)
 {
-    const double t0 = src_value(r.m.t0_src[q], theta, r.m.consts);
-    const float hi = (float)t0;
-    return make_float2(hi, (float)(t0 - (double)hi));
+    const dfl t0 = df_from_double(src_value(r.m.t0_src[q], theta, r.m.consts));
+    return make_float2(t0.h, t0.l);
 }
 
 // FP32 tables of proposal g from sm.theta[g] (sets sm.flag[g]).
