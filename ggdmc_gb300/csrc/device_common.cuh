@@ -257,6 +257,15 @@ __device__ __forceinline__ bool winner_br(const Ent32 &P, float uh, float ul, fl
         const float dP = fast ? tm - tz : phimax - tm, dp = pm - pz;
         br = fmaf(P.a.z, dP, fmaf(P.b.z, dP, dp));
         ref = 1.1e-16f * (fabsf(P.a.z) * phimax + pm + pz);
+        // A response far too fast for the winner (both z beyond 13): phi
+        // underflows FP32 there (phi(13) < 8.0e-38) and the bracket is at
+        // most (|kappa| / czm + 1) phi(czm).  When that bound puts the pdf
+        // below 1e-10, the reference's pdf (at most g phi(czm)) is floored
+        // too, so the trial takes the floor here instead of the FP64 form.
+        if (cmh > 13.f && P.c.x * fmaf(fabsf(P.a.z), 0.0769231f, 1.f) < 1.2e27f) {
+            br = __fdividef(1e-10f, P.c.x);
+            return true;
+        }
         if (!(br > 0.f) || !(br * kAmp >= fabsf(P.a.z * dP) + fabsf(dp))) return false;
     }
     const float pdf = br * P.c.x;

@@ -252,26 +252,35 @@ def test_edge_empty_subject_and_floor(oracle):
 
 
 def test_mixed_many_fallbacks_in_one_block(oracle):
-    # one subject of 3000 trials with t0 above a large share of its RTs: most
-    # trials leave the FP32 form (t < 1e-4), more than a block lists, so the
-    # block re-scans its trials; sums still match the FP64 oracle
+    # one subject of 3000 trials with drift rates 8x the generating ones: the
+    # responses are far too slow for them, so nearly every trial follows the
+    # reference form's FP64 rounding (a winner bracket of differences of Phi
+    # near 1, survivors of terms far above their size) and leaves the FP32
+    # form, more than a block lists, so the block re-scans its trials; sums
+    # still match the FP64 oracle.  And t0 above 60% of the RTs: those trials
+    # take the reference's floor, the ones just after t0 (a response far too
+    # fast for the winner) the floor by the bound on the bracket
     from ggdmc_gb300.design import T0_17_P, design_t0_17, vector
     rng = np.random.default_rng(21)
     model = design_t0_17()
     th = vector(model, T0_17_P)
     sub = synth.simulate_subject(model, th, 3000, rng, "1")
     batch = SubjectBatch.pack([sub])
-    bad = th.copy()
+    bad, late = th.copy(), th.copy()
     for j, nm in enumerate(model.pnames):
+        if nm.startswith("mean_v"):
+            bad[j] = 8.0 * th[j]
         if nm.startswith("t0"):
-            bad[j] = np.quantile(sub.rt, 0.6)
-    theta = np.stack([th, bad])[None]                  # [1][2][P]
+            late[j] = np.quantile(sub.rt, 0.6)
+    theta = np.stack([th, bad, late])[None]            # [1][3][P]
     h = gpu.Handle(model, batch)
     want = oracle.loglik(model, batch, theta)
     mixed = h.loglik(theta, abi.MIXED)
     assert np.all(rel(mixed, want) <= 1e-6), rel(mixed, want)
+    sums = h.loglik(theta, abi.MIXED_SUMS)
+    assert rel(sums[0, 2], want[0, 2]) <= 1e-6
     run = h.run(abi.DEConfigPy(nchain=3, nparameter=model.n_par, nmc=2, thin=1, seed=1,
-                               precision=abi.MIXED), synth.unif_prior(model.n_par),
+                               precision=abi.MIXED), synth.unif_prior(model.n_par, 0.0, 50.0),
                 np.stack([bad] * 3)[None], np.zeros((1, 3)), h.loglik(np.stack([bad] * 3)[None], abi.MIXED))
     assert run["stats"]["fallbacks"] > 1024
 
