@@ -141,9 +141,10 @@ __device__ __forceinline__ double lba_logdens64(double t, const int *ents, int K
 // the reference form: t < 1e-4; a winner bracket or survivor that cancels by
 // more than 16x; a pdf within 0.1% of the reference's 1e-10 floor (below it
 // the pdf is floored here); where the reference form's own FP64 rounding
-// exceeds 1e-8 relative (it differences Phi values near 1, or survivor terms
-// much larger than the survivor), so that the value follows the reference;
-// and a product outside the normal FP32 range.
+// exceeds 1e-6 relative in the winner's bracket (it differences Phi values
+// near 1) or 1e-8 in a survivor (terms much larger than the survivor), so
+// that the value follows the reference; and a product outside the normal
+// FP32 range.
 //
 // Per proposal and accumulator tuple (the host builds them in FP64):
 struct Ent32 {
@@ -273,7 +274,7 @@ __device__ __forceinline__ bool winner_br(const Ent32 &P, float uh, float ul, fl
         br = __fdividef(1e-10f, P.c.x);     // the reference's floor
         return true;
     }
-    return pdf >= 1.001e-10f && br * 1e-8f >= ref;
+    return pdf >= 1.001e-10f && br * 1e-6f >= ref;
 }
 
 // Survivor S of a losing accumulator; false: FP64 form.
