@@ -1749,8 +1749,14 @@ k_sub_step(RunDev r, int score_priors, int defer_next, int group)
             const int l = r.sub_order[s_q];
             if (vload(r.ready + l) == it + 1) {
                 __threadfence();                      // acquire l's proposals
-                const int k = atomicAdd(r.spec_cnt + l, 1);
-                if (k < n_item) s_m = spec_item_slots<true>(r, l, k, group, s_slots);
+                // two items a claim where their proposals fit one group:
+                // the resolve block's 16 warps then have twice the chunks
+                const int take = (2 * group <= kGroup) ? 2 : 1;
+                const int k = atomicAdd(r.spec_cnt + l, take);
+                int mm = 0;
+                for (int j = 0; j < take; ++j)
+                    if (k + j < n_item) mm += spec_item_slots<true>(r, l, k + j, group, s_slots + mm);
+                s_m = mm;
             }
         }
         __syncthreads();
