@@ -495,19 +495,23 @@ __device__ void ddm_build(const RunDev &r, SubSmem &sm, int g, const double *the
     }
 }
 
-// group_loglik for the diffusion model: FP32 per trial (MIXED) with FP64
-// re-evaluation where ddm_logdens32 declines, or FP64 throughout.
+// group_loglik for the diffusion model, into parts[g] (valid on all threads
+// on return).  MIXED: FP32 per trial with FP64 re-evaluation where
+// ddm_logdens32 declines, each term added in 2^-32 fixed point (an exact
+// integer sum, which no block size or grouping changes, as for the LBA);
+// FP64: a plain FP64 sum.
 __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem &sm, int ng, bool mixed,
-                                 double *out)
+                                 JobPart *parts)
 {
     for (int g = 0; g < ng; ++g) ddm_build(r, sm, g, sm.theta + g * kMaxTheta);
+    if (threadIdx.x < ng) parts[threadIdx.x] = JobPart{0, 0, 0, 0.0};
     __syncthreads();
     const int64_t base = r.offs[l] + i0;
     const int n = i1 - i0, K = r.m.n_acc, ND = r.m.n_dent;
     double acc[kGroup];
-    float ks[kGroup], kc[kGroup];
+    long long fx[kGroup];
 #pragma unroll
-    for (int g = 0; g < kGroup; ++g) { acc[g] = 0.0; ks[g] = 0.f; kc[g] = 0.f; }
+    for (int g = 0; g < kGroup; ++g) { acc[g] = 0.0; fx[g] = 0; }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int u = sm.cent[r.cell[base + i] * K];
         const float2 rt = r.rt32[base + i];
@@ -515,17 +519,23 @@ __device__ void ddm_group_loglik(const RunDev &r, int l, int i0, int i1, SubSmem
         for (int g = 0; g < kGroup; ++g) {
             if (g >= ng) break;
             float ld;
-            if (mixed && ddm_logdens32(rt.x, rt.y, sm.d32 + 8 * (g * ND + u), ld)) {
-                const float y = ld - kc[g];
-                const float tt = ks[g] + y;
-                kc[g] = (tt - ks[g]) - y;
-                ks[g] = tt;
-            } else {
+            if (!mixed) {
                 acc[g] += ddm_logdens64(r.rt64[base + i], sm.d64 + 8 * (g * ND + u));
+            } else if (ddm_logdens32(rt.x, rt.y, sm.d32 + 8 * (g * ND + u), ld)) {
+                fx[g] += __float2ll_rn(ld * kFixScale);          // |ld| < 89
+            } else {
+                const double x = ddm_logdens64(r.rt64[base + i], sm.d64 + 8 * (g * ND + u));
+                if (fabs(x) < 1073741824.0) fx[g] += __double2ll_rn(x * 4294967296.0);
+                else acc[g] += x;
             }
         }
     }
-    for (int g = 0; g < ng; ++g) out[g] = block_sum(acc[g] + ((double)ks[g] - (double)kc[g]), sm.red);
+    for (int g = 0; g < ng; ++g) {
+        if (mixed) warp_flush(parts[g], fx[g], 0, 0);
+        const double t = block_sum(acc[g], sm.red);   // its barriers also order the atomics
+        if (threadIdx.x == 0) parts[g].f64 = t;
+    }
+    __syncthreads();
 }
 
 // group_loglik's per-proposal results and partial sums, in sm.red after the
@@ -637,10 +647,7 @@ __device__ void group_chunk(const RunDev &r, int l, int i0, int i1, SubSmem &sm,
     bool ddm = MODEL == kDdmOnly;
     if constexpr (MODEL == kAnyModel) ddm = r.m.model_type == kModelDdm;
     if (ddm) {
-        double o[kGroup];
-        ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, o);
-        if (threadIdx.x < ng) parts[threadIdx.x] = JobPart{0, 0, 0, o[threadIdx.x]};
-        __syncthreads();
+        ddm_group_loglik(r, l, i0, i1, sm, ng, mixed, parts);
         return;
     }
     const int K = r.m.n_acc;

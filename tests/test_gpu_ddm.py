@@ -106,3 +106,27 @@ def test_ddm_hierarchical_fp64_bit_exact(oracle, work):
     assert np.array_equal(g["phi"][0], o["phi"][0])
     assert np.array_equal(g["subj"][0], o["subj"][0])
     np.testing.assert_allclose(g["subj"][2], o["subj"][2], rtol=1e-12)
+
+
+def test_ddm_mixed_same_decisions_under_both_schedules(monkeypatch, work):
+    # the ordered resolve (512-thread blocks) and the fused schedule take the
+    # same decisions on the diffusion model; its per-trial FP32 values may
+    # round differently in the two kernels (the compiler contracts its
+    # products and sums per kernel), so the sums agree to ~1e-6
+    w = work
+    S, C, P = w.batch.n_subject, 27, w.model.n_par
+    h = gpu.Handle(w.model, w.batch)
+    th = near_truth(w, C, 5)
+    lp = np.stack([gpu.logprior(w.p_prior, th[s]) for s in range(S)])
+    ll = h.loglik(th, abi.MIXED_SUMS)
+    cfg = abi.DEConfigPy(nchain=C, nparameter=P, nmc=6, thin=1, sub_migration_prob=0.2, seed=13,
+                         precision=abi.MIXED)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("GGDMC_FUSED", mode)
+        out[mode] = h.run(cfg, w.p_prior, th, lp, ll)
+    a, b = out["0"], out["1"]
+    np.testing.assert_array_equal(a["theta"], b["theta"])
+    np.testing.assert_array_equal(a["s_theta"], b["s_theta"])
+    np.testing.assert_allclose(a["ll"], b["ll"], rtol=0, atol=1e-5)
+    assert a["stats"]["accepts"] == b["stats"]["accepts"] > 0
