@@ -382,32 +382,8 @@ __device__ void build_tables64(const RunDev &r, SubSmem &sm, const double *theta
 __device__ __forceinline__ bool entry32(const RunDev &r, const double *theta, int u, Ent32 &E, double &lg)
 {
     const EntSrc es = r.m.ent_src[u];
-    const double A = src_value(es.A, theta, r.m.consts);
-    const double B = src_value(es.B, theta, r.m.consts);
-    const double v = src_value(es.v, theta, r.m.consts);
-    const double s = src_value(es.s, theta, r.m.consts);
-    const dfl Ad = df_from_double(A), Bd = df_from_double(B), sd = df_from_double(s);
-    const dfl is = df_div(dfl{1.f, 0.f}, sd);
-    const dfl kap = df_mul(df_from_double(v), is);
-    dfl den, qt;                                    // Phi(kappa), Phi(-kappa)
-    df_phi_pair(kap, den, qt);
-    const dfl g = df_div(sd, df_mul(Ad, den)), q = df_div(qt, den);
-    const dfl ab = df_mul(df_add(Ad, Bd), is), bs = df_mul(Bd, is), ha = df_mul_f(df_mul(Ad, is), 0.5f);
-    // (FP32 tests of A and s: a value too small for FP32 goes to the FP64 form)
-    const bool ok = Ad.h > 0.f && sd.h > 0.f && den.h > 1e-30f && isfinite(ab.h) && isfinite(bs.h) &&
-                    isfinite(kap.h) && isfinite(g.h) && isfinite(q.h) && ha.h > 0.f && g.h > 0.f;
-    const dfl lgd = ok ? df_log(g) : dfl{0.f, 0.f};
-    lg = df_to_double(lgd);
-    // the density floor of a trial before t0 in the trial form, less log g:
-    // log 1e-10 - log g = fe ln 2 + flm (fe an integer, |flm| <= ln 2 / 2),
-    // in double-float (log 1e-10 as hi + lo)
-    const dfl fx = df_add(dfl{-23.025850296020508f, -6.339199671856477e-07f}, df_neg(lgd));
-    const float fe = rintf(fx.h * 1.44269504088896341f);
-    const dfl fl = df_add(fx, df_neg(df_mul_f(dfl{kDfLn2H, kDfLn2L}, fe)));
-    E.a = make_float4(ab.h, fe, kap.h, ha.h);
-    E.b = make_float4(ab.l, fl.h + fl.l, kap.l, ha.l);
-    E.c = make_float4(g.h, g.l, q.h, q.l);
-    return ok;
+    return lba_tuple32(src_value(es.A, theta, r.m.consts), src_value(es.B, theta, r.m.consts),
+                       src_value(es.v, theta, r.m.consts), src_value(es.s, theta, r.m.consts), E, lg);
 }
 
 __device__ __forceinline__ float2 t0split(const RunDev &r, const double *theta, int q)
