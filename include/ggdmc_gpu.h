@@ -245,7 +245,9 @@ ggdmc_status ggdmc_loglik(ggdmc_handle *h, const double *theta, int32_t n_theta,
                           int32_t precision, double *out);
 
 /* The same with theta and out already in device memory (CUDA pointers) and
- * the launch on `stream` (a cudaStream_t; NULL = the default stream). */
+ * the launch on `stream` (a cudaStream_t; NULL = the default stream).  The
+ * handle keeps device buffers for the call (the proposals' FP32 tables at
+ * MIXED and MIXED_SUMS, the FP64 pass's work at MIXED), grown as needed. */
 ggdmc_status ggdmc_loglik_device(ggdmc_handle *h, const double *d_theta,
                                  int32_t n_theta, int32_t precision,
                                  double *d_out, void *stream);
