@@ -531,6 +531,24 @@ __device__ __forceinline__ float nf32_eval(const Nf32 &q, float w)
     return p * 3.14159265f;
 }
 
+// The diffusion entry of a responding boundary from its (a, v, z, d, sz, sv,
+// t0, st0): the upper boundary mirrored to the lower (v -> -v, z -> 1 - z),
+// the boundary's shift t0 -/+ d/2, in FP64 (e) and FP32 (f; f[7] the low
+// part of the shift).
+__device__ __forceinline__ void ddm_entry(const double *v8, bool upper, double *e, float *f)
+{
+    e[0] = v8[0];
+    e[1] = upper ? -v8[1] : v8[1];
+    e[2] = upper ? 1.0 - v8[2] : v8[2];
+    e[3] = upper ? v8[6] - v8[3] / 2.0 : v8[6] + v8[3] / 2.0;
+    e[4] = v8[4];
+    e[5] = v8[5];
+    e[6] = v8[7];
+    e[7] = 0.0;
+    for (int j = 0; j < 7; ++j) f[j] = (float)e[j];
+    f[7] = (float)(e[3] - (double)f[3]);
+}
+
 __device__ __forceinline__ bool ddm_logdens32(float rt_hi, float rt_lo, const float *p, float &ld)
 {
     const float a = p[0], v = p[1], zr = p[2], sz = p[4], sv = p[5], st0 = p[6];

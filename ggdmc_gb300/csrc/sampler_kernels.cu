@@ -455,19 +455,7 @@ __device__ void ddm_build(const RunDev &r, SubSmem &sm, int g, const double *the
         const int32_t *q = r.m.ddm_src + 9 * u;
         double v8[8];
         for (int j = 0; j < 8; ++j) v8[j] = src_value(q[j], theta, r.m.consts);
-        const bool upper = q[8] == 1;
-        double *e = sm.d64 + 8 * (g * ND + u);
-        e[0] = v8[0];
-        e[1] = upper ? -v8[1] : v8[1];
-        e[2] = upper ? 1.0 - v8[2] : v8[2];
-        e[3] = upper ? v8[6] - v8[3] / 2.0 : v8[6] + v8[3] / 2.0;
-        e[4] = v8[4];
-        e[5] = v8[5];
-        e[6] = v8[7];
-        e[7] = 0.0;
-        float *f = sm.d32 + 8 * (g * ND + u);
-        for (int j = 0; j < 7; ++j) f[j] = (float)e[j];
-        f[7] = (float)(e[3] - (double)f[3]);
+        ddm_entry(v8, q[8] == 1, sm.d64 + 8 * (g * ND + u), sm.d32 + 8 * (g * ND + u));
     }
 }
 

@@ -29,3 +29,18 @@ extern "C" int dc_trial(double rt, double t0, int K, const double *abvs, double 
     *logd = lgw + e * 0.6931471805599453 + (double)lm;
     return 0;
 }
+
+// One diffusion-model trial: the responding boundary's (a, v, z, d, sz, sv,
+// t0, st0) and whether it is the upper one.  0: the FP32 form's log density
+// in *logd; 1: the trial takes the FP64 form.
+extern "C" int dc_ddm(double rt, const double *v8, int upper, double *logd)
+{
+    double e[8];
+    float f[8];
+    ddm_entry(v8, upper != 0, e, f);
+    const float rh = (float)rt, rl = (float)(rt - (double)rh);
+    float ld;
+    if (!ddm_logdens32(rh, rl, f, ld)) return 1;
+    *logd = ld;
+    return 0;
+}

@@ -16,7 +16,9 @@ static inline float sinpif(float x) { return (float)sin(M_PI * (double)x); }
 static inline float rsqrtf(float x) { return 1.0f / sqrtf(x); }
 static inline float __frcp_rn(float x) { return 1.0f / x; }
 static inline float __fdividef(float a, float b) { return a / b; }
-// __logf: glibc's own (the natural log)
+// __logf: glibc declares a symbol of that name that it does not export
+static inline float ggdmc_host_logf(float x) { return logf(x); }
+#define __logf ggdmc_host_logf
 static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
 static inline float __int_as_float(int u) { float f; std::memcpy(&f, &u, 4); return f; }

@@ -40,6 +40,7 @@ def lib(tmp_path_factory):
     assert r.returncode == 0, r.stderr[-3000:]
     L = C.CDLL(so)
     L.dc_trial.argtypes = [C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.dc_ddm.argtypes = [C.c_double, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double)]
     return L
 
 
@@ -134,3 +135,40 @@ def test_responses_far_too_fast_take_the_floor(lib, oracle):
     assert fast.sum() > 20 and np.mean(codes[fast] == 0) >= 0.95
     assert np.all(np.abs(v[codes == 0] - want[codes == 0]) <= 2e-5)
     assert (codes != 0).mean() < 0.01
+
+
+def test_diffusion_fp32_density(lib, oracle):
+    """The diffusion model's FP32 density (Navarro-Fuss series, the sz / st0
+    midpoint rule) against the oracle's FP64 one on its benchmark design near
+    the generating values: per trial within 5e-5 (median 1e-6), few trials
+    left to FP64."""
+    w = synth.hier_ddm_64(n_subject=3, n=200, dt=1e-3)
+    m = w.model
+    rng = np.random.default_rng(6)
+    out = C.c_double()
+    errs, declined, n = [], 0, 0
+    for s in range(3):
+        a, b = w.batch.offsets[s], w.batch.offsets[s + 1]
+        for _ in range(2):
+            th = w.theta_true[s] * (1 + 0.05 * rng.standard_normal(m.n_par))
+            signed = np.array([nm.startswith("v.") for nm in m.pnames])
+            th = np.where(signed, th, np.abs(th))
+
+            def val(src):
+                return th[src] if src >= 0 else m.constants[-1 - src]
+
+            for i in range(a, b):
+                c = int(w.batch.cell[i])
+                wb = int(m.resp[c])
+                cv = np.array([[val(m.param_src[c, k, q]) for q in range(8)] for k in range(2)], np.float64)
+                v8 = np.ascontiguousarray(cv[wb])
+                code = lib.dc_ddm(float(w.batch.rt[i]), v8.ctypes.data_as(C.POINTER(C.c_double)), wb,
+                                  C.byref(out))
+                n += 1
+                if code:
+                    declined += 1
+                    continue
+                errs.append(out.value - np.log(oracle.ddm_dens(float(w.batch.rt[i]), cv, wb)))
+    err = np.abs(np.array(errs))
+    assert declined / n < 0.02
+    assert err.max() <= 5e-5 and np.median(err) <= 1e-6
