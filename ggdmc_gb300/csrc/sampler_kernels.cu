@@ -2585,8 +2585,9 @@ cudaError_t launch_sub_resolve(const RunDev &r, int pass, int level_begin, int l
                                bool score_priors, cudaStream_t st)
 {
     (void)pass;
-    // every subject at once: migration levels first, largest first, unless
-    // every level starts in the first wave; a single subject keeps its index
+    // every subject at once: migration levels first, then the others in
+    // res_order (by measured cost, else largest first), unless every level
+    // starts in the first wave; a single subject keeps its index
     thread_local int n_sm = 0;
     if (!n_sm) {
         int dev = 0;
